@@ -1,0 +1,174 @@
+"""ctypes binding of the oracle (oracle/_build/liborc.so).
+
+The oracle is the CPU restatement of the reference encoder; it is the checker
+the CUDA path is compared against and is used only by tests, smoke() and the
+CPU-baseline leg of bench.py.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(ROOT, "oracle", "_build", "liborc.so")
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+
+
+class Oracle:
+    def __init__(self, lib):
+        self.lib = lib
+        lib.orc_last_error.restype = ctypes.c_char_p
+        lib.orc_quality_to_lambda.restype = ctypes.c_double
+        lib.orc_norm97.restype = ctypes.c_double
+        lib.orc_time_encode.restype = ctypes.c_double
+        lib.orc_mq_encode.restype = _u8p
+
+    def _err(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what}: code {rc}: {self.lib.orc_last_error().decode()}")
+
+    def encode(self, px, w, h, ncomp, quality, fmt=0, threads=1, contrast_mask=False):
+        px = np.ascontiguousarray(px, dtype=np.uint8)
+        out = _u8p()
+        n = ctypes.c_size_t()
+        rc = self.lib.orc_encode(px.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint32(w),
+                                 ctypes.c_uint32(h), ncomp, quality, fmt, threads,
+                                 int(contrast_mask), ctypes.byref(out), ctypes.byref(n))
+        self._err(rc, "orc_encode")
+        data = ctypes.string_at(out, n.value)
+        self.lib.orc_free(out)
+        return data
+
+    def coefficients(self, px, w, h, ncomp, quality, comp):
+        px = np.ascontiguousarray(px, dtype=np.uint8)
+        out = np.zeros(w * h, np.int32)
+        rc = self.lib.orc_coefficients(px.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint32(w),
+                                       ctypes.c_uint32(h), ncomp, quality, comp,
+                                       out.ctypes.data_as(ctypes.c_void_p))
+        self._err(rc, "orc_coefficients")
+        return out.reshape(h, w)
+
+    def plan(self, w, h, ncomp, quality):
+        lv, cbw, nq = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        q = np.zeros(4 * 32, np.int32)
+        rc = self.lib.orc_plan(ctypes.c_uint32(w), ctypes.c_uint32(h), ncomp, quality,
+                               ctypes.byref(lv), ctypes.byref(cbw), ctypes.byref(nq),
+                               q.ctypes.data_as(ctypes.c_void_p))
+        self._err(rc, "orc_plan")
+        return {"levels": lv.value, "cbw": cbw.value,
+                "quants": [tuple(q[4 * i:4 * i + 4]) for i in range(nq.value)]}
+
+    def dwt(self, data, w, h, levels, kind, inverse=False):
+        if kind == 53:
+            a = np.ascontiguousarray(data, dtype=np.int32).copy()
+            f = self.lib.orc_inv53 if inverse else self.lib.orc_fwd53
+        else:
+            a = np.ascontiguousarray(data, dtype=np.float32).copy()
+            f = self.lib.orc_inv97 if inverse else self.lib.orc_fwd97
+        f(a.ctypes.data_as(ctypes.c_void_p), w, h, levels)
+        return a
+
+    def tables(self):
+        zc = np.zeros(2048, np.uint8)
+        sc = np.zeros(256, np.uint8)
+        spb = np.zeros(256, np.uint8)
+        mq = np.zeros(94 * 4, np.uint16)
+        self.lib.orc_tables(*(a.ctypes.data_as(ctypes.c_void_p) for a in (zc, sc, spb, mq)))
+        return zc, sc, spb, mq
+
+    def mq_encode(self, syms, variant=0):
+        syms = np.ascontiguousarray(syms, dtype=np.uint8)
+        n = ctypes.c_size_t()
+        p = self.lib.orc_mq_encode(syms.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(syms.size),
+                                   variant, ctypes.byref(n))
+        data = ctypes.string_at(p, n.value)
+        self.lib.orc_free(p)
+        return data
+
+    def mq_decode(self, data, ctxs):
+        ctxs = np.ascontiguousarray(ctxs, dtype=np.uint8)
+        bits = np.zeros(ctxs.size, np.uint8)
+        self.lib.orc_mq_decode(data, ctypes.c_size_t(len(data)), ctxs.ctypes.data_as(ctypes.c_void_p),
+                               ctypes.c_size_t(ctxs.size), bits.ctypes.data_as(ctypes.c_void_p))
+        return bits
+
+    def t1_block(self, coefs, w, h, band, mb):
+        coefs = np.ascontiguousarray(coefs, dtype=np.int32)
+        mbp, zbp, cls, npasses = (ctypes.c_int() for _ in range(4))
+        cap = 128
+        passes = np.zeros(6 * cap, np.int32)
+        out = _u8p()
+        n = ctypes.c_size_t()
+        rc = self.lib.orc_t1_block(coefs.ctypes.data_as(ctypes.c_void_p), w, h, band, mb,
+                                   ctypes.byref(mbp), ctypes.byref(zbp), ctypes.byref(cls),
+                                   ctypes.byref(npasses), passes.ctypes.data_as(ctypes.c_void_p),
+                                   cap, ctypes.byref(out), ctypes.byref(n))
+        self._err(rc, "orc_t1_block")
+        payload = ctypes.string_at(out, n.value)
+        self.lib.orc_free(out)
+        return {"mbp": mbp.value, "zbp": zbp.value, "cls": cls.value,
+                "passes": passes[:6 * npasses.value].reshape(-1, 6), "payload": payload}
+
+    def t1_decode(self, data, w, h, band, mb, zbp, npasses):
+        out = np.zeros(w * h, np.int32)
+        rc = self.lib.orc_t1_decode(data, ctypes.c_size_t(len(data)), w, h, band, mb, zbp, npasses,
+                                    out.ctypes.data_as(ctypes.c_void_p))
+        if rc != 0:
+            raise RuntimeError(f"orc_t1_decode: code {rc}")
+        return out
+
+    def block_summary(self, px, w, h, ncomp, quality, pcrd=True):
+        px = np.ascontiguousarray(px, dtype=np.uint8)
+        cap = 1 << 20
+        rows = np.zeros(9 * cap, np.int32)
+        n = ctypes.c_int()
+        rc = self.lib.orc_block_summary(px.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint32(w),
+                                        ctypes.c_uint32(h), ncomp, quality, int(pcrd),
+                                        rows.ctypes.data_as(ctypes.c_void_p), cap, ctypes.byref(n))
+        self._err(rc, "orc_block_summary")
+        return rows[:9 * n.value].reshape(-1, 9)
+
+    def decode(self, data):
+        w, h, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int()
+        rc = self.lib.orc_decode(data, ctypes.c_size_t(len(data)), ctypes.byref(w), ctypes.byref(h),
+                                 ctypes.byref(c), None, ctypes.c_size_t(0))
+        self._err(rc, "orc_decode")
+        px = np.zeros(w.value * h.value * c.value, np.uint8)
+        rc = self.lib.orc_decode(data, ctypes.c_size_t(len(data)), ctypes.byref(w), ctypes.byref(h),
+                                 ctypes.byref(c), px.ctypes.data_as(ctypes.c_void_p),
+                                 ctypes.c_size_t(px.size))
+        self._err(rc, "orc_decode")
+        return w.value, h.value, c.value, px
+
+    def quality_metrics(self, px, w, h, ncomp, quality):
+        px = np.ascontiguousarray(px, dtype=np.uint8)
+        psnr, ssim = ctypes.c_double(), ctypes.c_double()
+        rc = self.lib.orc_quality_metrics(px.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint32(w),
+                                          ctypes.c_uint32(h), ncomp, quality, ctypes.byref(psnr),
+                                          ctypes.byref(ssim))
+        self._err(rc, "orc_quality_metrics")
+        return psnr.value, ssim.value
+
+    def time_encode(self, px, w, h, ncomp, quality, fmt, threads, contrast_mask, iters):
+        px = np.ascontiguousarray(px, dtype=np.uint8)
+        return self.lib.orc_time_encode(px.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint32(w),
+                                        ctypes.c_uint32(h), ncomp, quality, fmt, threads,
+                                        int(contrast_mask), iters)
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+
+
+_cached = None
+
+
+def load():
+    global _cached
+    if _cached is None:
+        if not os.path.exists(LIB):
+            build()
+        _cached = Oracle(ctypes.CDLL(LIB))
+    return _cached
