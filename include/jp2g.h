@@ -1,0 +1,107 @@
+/*
+ * jp2g — GB300-native JPEG 2000 encode engine, C ABI.
+ *
+ * The drop-in boundary for jp2lam's encode path. A Rust (or any FFI) host
+ * keeps jp2lam's public types (Image, EncodeOptions, BatchEncoder) and calls
+ * these entry points instead of NativeBackend; see INTEGRATION.md for the
+ * extern "C" binding. Plain pointers and sizes only.
+ *
+ * Status codes map 1:1 to jp2lam::Jp2LamError (src/error.rs:7-13):
+ *   0 ok, 1 InvalidInput, 2 EncodeFailed, 3 DecodeFailed,
+ *   4 UnsupportedFeature, 5 Io.
+ * Every entry point validates its arguments before any device work; a failed
+ * call leaves a message for jp2g_last_error(). There is no CPU fallback: a
+ * context cannot be created without a usable CUDA device.
+ */
+#ifndef JP2G_H
+#define JP2G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct jp2g_ctx jp2g_ctx;
+
+enum {
+  JP2G_OK = 0,
+  JP2G_INVALID_INPUT = 1,
+  JP2G_ENCODE_FAILED = 2,
+  JP2G_DECODE_FAILED = 3,
+  JP2G_UNSUPPORTED_FEATURE = 4,
+  JP2G_IO = 5
+};
+
+enum { JP2G_FORMAT_J2K = 0, JP2G_FORMAT_JP2 = 1 };
+
+/* One engine per process and GPU. Owns a CUDA stream and device buffer pools
+ * that grow on demand up to `hbm_budget_bytes` (0 = no limit).
+ * Replaces the construction of NativeBackend (src/encode/backend/mod.rs:6-9;
+ * src/encode/mod.rs:87). */
+int jp2g_create(jp2g_ctx** ctx, int device, uint64_t hbm_budget_bytes);
+void jp2g_destroy(jp2g_ctx* ctx);
+
+/* Encode one 8-bit page: ncomp 1 (gray) or 3 (sRGB); `interleaved` selects
+ * RGBRGB... (as Image::from_rgb_bytes takes, src/model.rs:87-117) or three
+ * planes; quality 0..100 (100 = lossless 5/3); format JP2G_FORMAT_*.
+ * On success *out holds a malloc'd J2K/JP2 byte string (free with
+ * jp2g_free) byte-identical to jp2lam::encode (src/encode/mod.rs:84-101).
+ * Replaces NativeBackend::encode_codestream (src/encode/backend/native/
+ * backend.rs:32-40) plus the JP2 wrap (src/jp2.rs:13-50). */
+int jp2g_encode(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h, uint32_t ncomp,
+                int interleaved, uint8_t quality, int format, uint8_t** out, size_t* out_len);
+
+/* Same as jp2g_encode, but `d_px` is interleaved pixel data already resident
+ * in device memory (w * h * ncomp bytes). Used for device-resident batching;
+ * the reference has no equivalent entry point (its input is always host
+ * memory). */
+int jp2g_encode_device(jp2g_ctx* ctx, const uint8_t* d_px, uint32_t w, uint32_t h,
+                       uint32_t ncomp, uint8_t quality, int format, uint8_t** out,
+                       size_t* out_len);
+
+void jp2g_free(uint8_t* p);
+
+/* Message of the last failed call on this context (or of the last failed
+ * jp2g_create when ctx is NULL). */
+const char* jp2g_last_error(jp2g_ctx* ctx);
+
+/* Device stream the context launches on (a cudaStream_t), for callers that
+ * time or order their own work against the engine. */
+void* jp2g_stream(jp2g_ctx* ctx);
+
+/* Stage timings of the last encode, in milliseconds, measured with CUDA
+ * events on the context's stream when timing is enabled:
+ * [0] h2d, [1] dwt (all levels), [2] tier-1, [3] pcrd, [4] compaction,
+ * [5] d2h, [6] host tier-2 + codestream, [7] total. Returns the count. */
+int jp2g_set_timing(jp2g_ctx* ctx, int enabled);
+int jp2g_stage_times(jp2g_ctx* ctx, float* ms, int n);
+
+/* Work counters of the last encode: [0] code-blocks, [1] non-empty blocks,
+ * [2] coding passes, [3] payload bytes before rate control, [4] bytes
+ * retained, [5] kernel launches, [6] coefficient bit-planes
+ * (sum over blocks of coefficients x magnitude bit-planes). */
+int jp2g_counters(jp2g_ctx* ctx, uint64_t* out, int n);
+
+/* Inspection entry points for parity tests. */
+/* Quantised coefficient plane (Mallat layout, w*h int32) of component
+ * `comp` after colour transform, DWT and quantisation. */
+int jp2g_debug_coefficients(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,
+                            uint32_t ncomp, uint8_t quality, uint32_t comp, int32_t* plane);
+/* Per-block Tier-1 results in codestream order, 8 int32 per block:
+ * (mbp, zbp, npasses, payload_len, cls, status, kept_passes, kept_bytes). */
+int jp2g_debug_blocks(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,
+                      uint32_t ncomp, uint8_t quality, int32_t* rows, uint32_t cap,
+                      uint32_t* nblocks);
+
+/* Host-only, no device needed: the Tier-1 context tables (zero coding
+ * 4x512, sign context 256, sign prediction 256) and the MQ state table
+ * (94 entries, qe | next_mps << 16 | next_lps << 24) the kernels use. */
+void jp2g_tables(uint8_t* zc, uint8_t* sc, uint8_t* spb, uint32_t* mq);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JP2G_H */

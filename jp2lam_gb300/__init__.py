@@ -1,0 +1,202 @@
+"""jp2lam_gb300 — GB300-native JPEG 2000 encoder with jp2lam's encode API.
+
+Python mirror of the reference's public encode surface (src/lib.rs:19-29),
+backed by the C ABI in include/jp2g.h (libjp2g.so, CUDA for sm_103a):
+
+    Image.from_gray_bytes / Image.from_rgb_bytes   (src/model.rs:87-140)
+    EncodeOptions(quality, format), Preset          (src/model.rs:41-177)
+    encode(image, options) -> bytes                 (src/encode/mod.rs:84-101)
+    encode_to_writer(image, options, writer)        (src/encode/mod.rs:103-113)
+    BatchEncoder(options).encode_one / encode_all   (src/batch.rs:26-85)
+    encode_batch(images, options)                   (src/batch.rs:173-178)
+
+Errors are Jp2LamError subclasses carrying the reference's variant names.
+The compute path is the CUDA library only; if it cannot be loaded or no GPU
+is present, encoding raises instead of falling back to the CPU.
+"""
+from __future__ import annotations
+
+import enum
+from dataclasses import dataclass, field
+from typing import Iterable, List, Optional
+
+from ._native import Engine, Jp2LamError, InvalidInput, EncodeFailed, DecodeFailed, \
+    UnsupportedFeature, IoError, default_engine
+
+__all__ = [
+    "ColorSpace", "OutputFormat", "Preset", "Image", "Component", "EncodeOptions",
+    "encode", "encode_to_writer", "BatchEncoder", "BatchProfile", "encode_batch",
+    "Engine", "Jp2LamError", "InvalidInput", "EncodeFailed", "DecodeFailed",
+    "UnsupportedFeature", "IoError",
+]
+
+
+class ColorSpace(enum.Enum):
+    GRAY = "Gray"
+    SRGB = "Srgb"
+
+    def component_count(self) -> int:
+        return 1 if self is ColorSpace.GRAY else 3
+
+
+class OutputFormat(enum.IntEnum):
+    J2K = 0
+    JP2 = 1
+
+
+class Preset(enum.Enum):
+    """src/model.rs:41-62"""
+    DOCUMENT_LOW = 30
+    DOCUMENT_HIGH = 85
+    WEB_LOW = 42
+    WEB_HIGH = 62
+
+    def quality(self) -> int:
+        return self.value
+
+
+@dataclass
+class Component:
+    width: int
+    height: int
+    precision: int = 8
+    signed: bool = False
+    dx: int = 1
+    dy: int = 1
+
+
+@dataclass
+class Image:
+    """Interleaved 8-bit pixels plus the reference Image's metadata."""
+    width: int
+    height: int
+    colorspace: ColorSpace
+    data: bytes
+    components: List[Component] = field(default_factory=list)
+
+    @staticmethod
+    def from_gray_bytes(width: int, height: int, data) -> "Image":
+        data = bytes(data)
+        expected = width * height
+        if len(data) != expected:
+            raise InvalidInput(
+                f"Gray buffer length {len(data)} does not match {width}×{height}={expected}")
+        return Image(width, height, ColorSpace.GRAY, data, [Component(width, height)])
+
+    @staticmethod
+    def from_rgb_bytes(width: int, height: int, data) -> "Image":
+        data = bytes(data)
+        expected = width * height * 3
+        if len(data) != expected:
+            raise InvalidInput(
+                f"RGB buffer length {len(data)} does not match {width}×{height}×3={expected}")
+        return Image(width, height, ColorSpace.SRGB, data, [Component(width, height) for _ in range(3)])
+
+    @property
+    def ncomp(self) -> int:
+        return self.colorspace.component_count()
+
+
+@dataclass
+class EncodeOptions:
+    """src/model.rs:156-177 (default: DocumentHigh quality, JP2)."""
+    quality: int = 85
+    format: OutputFormat = OutputFormat.JP2
+
+    @staticmethod
+    def from_preset(preset: Preset, fmt: OutputFormat) -> "EncodeOptions":
+        return EncodeOptions(preset.quality(), fmt)
+
+
+def _validate(image: Image) -> None:
+    # validate_image (src/plan/validate.rs:4-62)
+    if image.width == 0 or image.height == 0:
+        raise InvalidInput("image dimensions must be non-zero")
+    if len(image.components) != image.colorspace.component_count():
+        raise InvalidInput(f"{image.colorspace.value} images must have exactly "
+                           f"{image.colorspace.component_count()} component(s)")
+    for idx, c in enumerate(image.components):
+        if c.width != image.width or c.height != image.height:
+            raise InvalidInput(f"component {idx} dimensions {c.width}x{c.height} do not match "
+                               f"image {image.width}x{image.height}")
+        if c.precision != 8:
+            raise InvalidInput(f"component {idx} precision {c.precision} is unsupported; "
+                               "only 8-bit is supported")
+        if c.signed:
+            raise InvalidInput(f"component {idx} must be unsigned")
+        if c.dx != 1 or c.dy != 1:
+            raise InvalidInput(f"component {idx} subsampling {c.dx}x{c.dy} is unsupported")
+    if len(image.data) != image.width * image.height * image.ncomp:
+        raise InvalidInput("pixel buffer length does not match the image dimensions")
+
+
+def encode(image: Image, options: Optional[EncodeOptions] = None,
+           engine: Optional[Engine] = None) -> bytes:
+    """Encode one page on the GPU; byte-identical to jp2lam::encode."""
+    options = options or EncodeOptions()
+    _validate(image)
+    eng = engine or default_engine()
+    return eng.encode(image.data, image.width, image.height, image.ncomp,
+                      int(options.quality), int(options.format))
+
+
+def encode_to_writer(image: Image, options: EncodeOptions, writer) -> None:
+    data = encode(image, options)
+    try:
+        writer.write(data)
+    except Exception as err:  # mirrors EncodeFailed(err.to_string())
+        raise EncodeFailed(str(err)) from err
+
+
+@dataclass(frozen=True)
+class BatchProfile:
+    """src/batch.rs:5-24"""
+    width: int
+    height: int
+    colorspace: ColorSpace
+    components: tuple
+    quality: int
+    format: OutputFormat
+
+    @staticmethod
+    def from_image(image: Image, options: EncodeOptions) -> "BatchProfile":
+        comps = tuple((c.width, c.height, c.precision, c.signed, c.dx, c.dy) for c in image.components)
+        return BatchProfile(image.width, image.height, image.colorspace, comps,
+                            int(options.quality), OutputFormat(options.format))
+
+
+class BatchEncoder:
+    """src/batch.rs:26-85: pins the profile of the first image and rejects
+    mismatches; every page is encoded on the GPU."""
+
+    def __init__(self, options: Optional[EncodeOptions] = None, engine: Optional[Engine] = None):
+        self.options = options or EncodeOptions()
+        self._profile: Optional[BatchProfile] = None
+        self._count = 0
+        self._engine = engine
+
+    def profile(self) -> Optional[BatchProfile]:
+        return self._profile
+
+    def encoded_count(self) -> int:
+        return self._count
+
+    def _validate_or_set_profile(self, image: Image) -> None:
+        prof = BatchProfile.from_image(image, self.options)
+        if self._profile is None:
+            self._profile = prof
+        elif self._profile != prof:
+            raise InvalidInput(f"batch item profile mismatch: expected {self._profile}, found {prof}")
+
+    def encode_one(self, image: Image) -> bytes:
+        self._validate_or_set_profile(image)
+        out = encode(image, self.options, self._engine)
+        self._count += 1
+        return out
+
+    def encode_all(self, images: Iterable[Image]) -> List[bytes]:
+        return [self.encode_one(im) for im in images]
+
+
+def encode_batch(images: Iterable[Image], options: EncodeOptions) -> List[bytes]:
+    return BatchEncoder(options).encode_all(images)

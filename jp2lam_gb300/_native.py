@@ -1,0 +1,234 @@
+"""ctypes binding of libjp2g.so (the C ABI declared in include/jp2g.h).
+
+The library is built in-tree by jp2lam_gb300/build.py. Loading never falls
+back to anything else: a missing library or a missing GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libjp2g.so")
+SYNTH_PATH = os.path.join(HERE, "_lib", "libjp2g_synth.so")
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+
+
+class Jp2LamError(Exception):
+    """Base of the reference's error variants (src/error.rs:7-13)."""
+    code = 2
+
+
+class InvalidInput(Jp2LamError):
+    code = 1
+
+
+class EncodeFailed(Jp2LamError):
+    code = 2
+
+
+class DecodeFailed(Jp2LamError):
+    code = 3
+
+
+class UnsupportedFeature(Jp2LamError):
+    code = 4
+
+
+class IoError(Jp2LamError):
+    code = 5
+
+
+_BY_CODE = {1: InvalidInput, 2: EncodeFailed, 3: DecodeFailed, 4: UnsupportedFeature, 5: IoError}
+
+# Every symbol the header declares (checked by the CPU test-suite).
+EXPORTS = [
+    "jp2g_create", "jp2g_destroy", "jp2g_encode", "jp2g_encode_device", "jp2g_free",
+    "jp2g_last_error", "jp2g_stream", "jp2g_set_timing", "jp2g_stage_times", "jp2g_counters",
+    "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_tables",
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libjp2g.so and declares its signatures. Raises if it is absent."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise EncodeFailed(f"CUDA engine library not built: {path} (run jp2lam_gb300/build.py)")
+        lib = ctypes.CDLL(path)
+        lib.jp2g_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_uint64]
+        lib.jp2g_destroy.argtypes = [ctypes.c_void_p]
+        lib.jp2g_encode.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_uint32, ctypes.c_int, ctypes.c_uint8, ctypes.c_int,
+                                    ctypes.POINTER(_u8p), ctypes.POINTER(ctypes.c_size_t)]
+        lib.jp2g_encode_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8, ctypes.c_int,
+                                           ctypes.POINTER(_u8p), ctypes.POINTER(ctypes.c_size_t)]
+        lib.jp2g_free.argtypes = [_u8p]
+        lib.jp2g_last_error.argtypes = [ctypes.c_void_p]
+        lib.jp2g_last_error.restype = ctypes.c_char_p
+        lib.jp2g_stream.argtypes = [ctypes.c_void_p]
+        lib.jp2g_stream.restype = ctypes.c_void_p
+        lib.jp2g_set_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.jp2g_stage_times.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib.jp2g_counters.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib.jp2g_debug_coefficients.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                                ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8,
+                                                ctypes.c_uint32, ctypes.c_void_p]
+        lib.jp2g_debug_blocks.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8,
+                                          ctypes.c_void_p, ctypes.c_uint32,
+                                          ctypes.POINTER(ctypes.c_uint32)]
+        lib.jp2g_tables.argtypes = [ctypes.c_void_p] * 4
+        _lib = lib
+        return lib
+
+
+def _raise(code: int, msg: str):
+    raise _BY_CODE.get(code, Jp2LamError)(msg)
+
+
+class Engine:
+    """One jp2g context (CUDA stream + device pools) on one GPU."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.jp2g_create(ctypes.byref(h), device, hbm_budget_bytes)
+        if rc != 0:
+            _raise(rc, self.lib.jp2g_last_error(None).decode())
+        self.handle = h
+        self._lock = threading.Lock()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.jp2g_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            _raise(rc, self.lib.jp2g_last_error(self.handle).decode())
+
+    def encode(self, px, w: int, h: int, ncomp: int, quality: int, fmt: int,
+               interleaved: bool = True) -> bytes:
+        buf = np.frombuffer(px, dtype=np.uint8) if isinstance(px, (bytes, bytearray)) else \
+            np.ascontiguousarray(px, dtype=np.uint8)
+        if buf.size != w * h * ncomp:
+            raise InvalidInput("pixel buffer length does not match the image dimensions")
+        out = _u8p()
+        n = ctypes.c_size_t()
+        with self._lock:
+            rc = self.lib.jp2g_encode(self.handle, buf.ctypes.data_as(ctypes.c_void_p), w, h, ncomp,
+                                      int(interleaved), quality, fmt, ctypes.byref(out), ctypes.byref(n))
+            self._check(rc)
+        data = ctypes.string_at(out, n.value)
+        self.lib.jp2g_free(out)
+        return data
+
+    def encode_device(self, dev_ptr: int, w: int, h: int, ncomp: int, quality: int, fmt: int) -> bytes:
+        out = _u8p()
+        n = ctypes.c_size_t()
+        with self._lock:
+            rc = self.lib.jp2g_encode_device(self.handle, ctypes.c_void_p(dev_ptr), w, h, ncomp, quality,
+                                             fmt, ctypes.byref(out), ctypes.byref(n))
+            self._check(rc)
+        data = ctypes.string_at(out, n.value)
+        self.lib.jp2g_free(out)
+        return data
+
+    def stream(self) -> int:
+        return self.lib.jp2g_stream(self.handle)
+
+    def set_timing(self, on: bool):
+        self.lib.jp2g_set_timing(self.handle, int(on))
+
+    def stage_times(self):
+        ms = (ctypes.c_float * 8)()
+        self.lib.jp2g_stage_times(self.handle, ms, 8)
+        keys = ["h2d", "dwt", "tier1", "pcrd", "compact", "d2h", "host_t2", "total"]
+        return dict(zip(keys, list(ms)))
+
+    def counters(self):
+        c = (ctypes.c_uint64 * 8)()
+        self.lib.jp2g_counters(self.handle, c, 8)
+        return list(c)
+
+    def debug_coefficients(self, px, w, h, ncomp, quality, comp):
+        px = np.ascontiguousarray(px, dtype=np.uint8)
+        plane = np.zeros(w * h, np.int32)
+        self._check(self.lib.jp2g_debug_coefficients(self.handle, px.ctypes.data_as(ctypes.c_void_p), w, h,
+                                                     ncomp, quality, comp,
+                                                     plane.ctypes.data_as(ctypes.c_void_p)))
+        return plane.reshape(h, w)
+
+    def debug_blocks(self, px, w, h, ncomp, quality):
+        px = np.ascontiguousarray(px, dtype=np.uint8)
+        n = ctypes.c_uint32()
+        self._check(self.lib.jp2g_debug_blocks(self.handle, px.ctypes.data_as(ctypes.c_void_p), w, h, ncomp,
+                                               quality, None, 0, ctypes.byref(n)))
+        rows = np.zeros(8 * n.value, np.int32)
+        self._check(self.lib.jp2g_debug_blocks(self.handle, px.ctypes.data_as(ctypes.c_void_p), w, h, ncomp,
+                                               quality, rows.ctypes.data_as(ctypes.c_void_p), n.value,
+                                               ctypes.byref(n)))
+        return rows.reshape(-1, 8)
+
+
+def tables():
+    """The Tier-1/MQ tables the kernels use (host-only, no GPU needed)."""
+    lib = load_library()
+    zc = np.zeros(2048, np.uint8)
+    sc = np.zeros(256, np.uint8)
+    spb = np.zeros(256, np.uint8)
+    mq = np.zeros(94, np.uint32)
+    lib.jp2g_tables(*(a.ctypes.data_as(ctypes.c_void_p) for a in (zc, sc, spb, mq)))
+    return zc, sc, spb, mq
+
+
+_default = None
+
+
+def default_engine() -> Engine:
+    global _default
+    with _lock:
+        if _default is None:
+            _default = Engine(0)
+        return _default
+
+
+# ------------------------------------------------------------- synthetic ----
+_synth = None
+
+
+def synth_page(w: int, h: int, ncomp: int, seed: int, glyphs: int = -1, photo_w: int = 0,
+               photo_h: int = 0, photo_frac: float = 0.0) -> np.ndarray:
+    """Seeded synthetic document page, interleaved uint8 (h, w, ncomp)."""
+    global _synth
+    if _synth is None:
+        if not os.path.exists(SYNTH_PATH):
+            from . import build as _b
+            _b.build_synth()
+        _synth = ctypes.CDLL(SYNTH_PATH)
+        _synth.jp2g_synth_page.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                           ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_double]
+    out = np.zeros(w * h * ncomp, np.uint8)
+    rc = _synth.jp2g_synth_page(out.ctypes.data_as(ctypes.c_void_p), w, h, ncomp, ctypes.c_uint64(seed),
+                                glyphs, photo_w, photo_h, photo_frac)
+    if rc < 0:
+        raise InvalidInput("bad synthetic page parameters")
+    return out

@@ -1,0 +1,75 @@
+// Kernel launch interfaces (device side of the pipeline).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "jp2g_internal.h"
+
+namespace jp2g {
+
+// Where one subband of one component lands in code-block storage.
+struct DwtBandOut {
+  uint32_t first_block;
+  int ncbx;
+  float step;  // quantiser step (irreversible path)
+};
+
+struct DwtLevelArgs {
+  // Input: the page's pixels (first level) or the previous level's LL plane.
+  int from_pixels;
+  const uint8_t* px;
+  size_t px_pitch;  // bytes per pixel row
+  int mct;          // apply RCT/ICT (three interleaved components)
+  const void* src;  // previous LL plane (int32 or float), component-major
+  size_t src_pitch, src_comp;
+  int ncomp;
+  int rw, rh;        // region size at this level
+  int no_transform;  // zero decomposition levels: copy (and quantise) only
+  // Output: next LL plane, or nullptr to send LL to code-block storage.
+  void* ll;
+  size_t ll_pitch, ll_comp;
+  int32_t* coef;
+  int cbw, cbh;
+  DwtBandOut band[3][4];
+};
+
+void launch_dwt_level(const DwtLevelArgs& a, bool reversible, cudaStream_t st);
+
+struct T1Args {
+  const BlockDesc* blocks;
+  uint32_t nblocks;
+  const int32_t* coef;
+  int cbw, cbh;
+  uint8_t* out;
+  PassRec* passes;
+  uint32_t pass_cap;  // pass records available per block
+  BlockOut* res;
+};
+
+void launch_t1(const T1Args& a, int num_sms, cudaStream_t st);
+
+struct PcrdArgs {
+  const BlockDesc* blocks;
+  uint32_t nblocks;
+  const BlockOut* res;
+  const PassRec* passes;
+  const BandParam* bands;
+  const CompParam* comps;
+  unsigned long long* comp_max_slope;  // f64 bit patterns (non-negative)
+  uint32_t ncomp_keys;
+  uint16_t* hull_passes;  // per pass slot
+  double* hull_slope;
+  uint8_t* hull_n;        // hull points per block
+  BlockKeep* keep;
+};
+
+void launch_pcrd(const PcrdArgs& a, cudaStream_t st);
+
+// Packs the retained payload bytes of every block, in work-list order, into
+// `dst`; offsets[b] receives the byte offset of block b and offsets[n] the
+// total. `scratch` holds ceil(n/1024)+1 uint32.
+void launch_compact(const BlockDesc* blocks, const BlockKeep* keep, uint32_t nblocks,
+                    const uint8_t* src, uint8_t* dst, uint32_t* offsets, uint32_t* scratch,
+                    cudaStream_t st);
+
+}  // namespace jp2g
