@@ -1,0 +1,284 @@
+"""Benchmark: encode MPix/s and page latency of the JPEG 2000 encoder on GB300.
+
+Workload (default): one 2550x3300 8-bit grayscale synthetic document page
+(text lines + an 800x600 blurred-noise photo region) encoded at quality 85
+(lossy 9/7, 5 levels, 64x64 code-blocks) to JP2 per step, on the plain
+per-page GPU path. Inputs are seeded synthetic pages (no dataset).
+
+value : MPix/s with the page already resident in HBM (jp2g_encode_device),
+        whole job: DWT, Tier-1, PCRD, compaction, read-back, host Tier-2.
+e2e   : the same through the C ABI with host buffers (jp2g_encode): the
+        host->device copy of the page and the device->host read of the
+        result are inside the timed region.
+Each step is timed with CUDA events on the engine's stream; between steps
+the L2 is flushed by writing a 256 MiB buffer (outside the timed events).
+
+--impl reference times the CPU restatement of the reference encoder (the
+reference Rust crate cannot be built here: no Rust toolchain, and its
+rayon/wide dependencies are not vendored) on the host cores, same workload.
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H, NCOMP, QUALITY, FMT = 2550, 3300, 1, 85, 1
+METRIC = "encode MPix/s (2550x3300 gray q85 JP2, plain per-page GPU path)"
+CONFIG = {"workload": "2550x3300 8-bit gray synthetic document page (text + 800x600 photo), "
+                      "quality 85 (9/7, 5 levels, 64x64 code-blocks) -> JP2, one page per step",
+          "pages_per_step": 1, "l2": "flushed between steps (256 MiB write)"}
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "fallback": True}
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the
+    timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[2:]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(px, iters, threads, contrast_mask):
+    from tests import oracle_lib
+    orc = oracle_lib.load()
+    sec = orc.time_encode(px, W, H, NCOMP, QUALITY, FMT, threads, contrast_mask, iters)
+    return (W * H / 1e6) / sec, sec
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from jp2lam_gb300._native import synth_page
+    px = synth_page(W, H, NCOMP, 1, photo_w=800, photo_h=600)
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup + args.steps):
+        v, _ = cpu_baseline(px, 1, threads, False)
+        vals.append(v)
+    vals = vals[args.warmup:]
+    value = float(np.mean(vals))
+    shipped, _ = cpu_baseline(px, 1, threads, True)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "MPix/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": W * H / 1e6 / value * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/i32", "data": "synthetic", "config": CONFIG,
+            "cpu_baseline": {"value": value, "unit": "MPix/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full 2550x3300 pages, one encode each, "
+                                       "all host threads; reference-as-shipped (with its unused "
+                                       f"contrast-mask DCT) = {shipped:.3f} MPix/s",
+                             "value_as_shipped": shipped},
+            "e2e": {"value": value, "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+        td.init_process_group("nccl" if args.impl != "reference" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist:
+            td.destroy_process_group()
+        return
+
+    import torch
+    import jp2lam_gb300 as jl
+    from jp2lam_gb300._native import synth_page
+
+    torch.cuda.set_device(local)
+    eng = jl.Engine(local)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=local)
+    eng.set_timing(True)
+    # per-rank page (weak scaling: every rank encodes its own pages)
+    px = synth_page(W, H, NCOMP, 1 + rank, photo_w=800, photo_h=600)
+    d_px = torch.from_numpy(px).to(f"cuda:{local}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+
+    def timed(fn, steps):
+        times, stages, outs = [], [], []
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for i in range(steps):
+            flush_l2()
+            starts[i].record(stream)
+            out = fn()
+            ends[i].record(stream)
+            outs.append(len(out))
+            stages.append(eng.stage_times())
+        torch.cuda.synchronize()
+        times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        return times, stages, outs
+
+    dev_fn = lambda: eng.encode_device(d_px.data_ptr(), W, H, NCOMP, QUALITY, FMT)
+    host_fn = lambda: eng.encode(px, W, H, NCOMP, QUALITY, FMT)
+    for _ in range(args.warmup):
+        dev_fn()
+        host_fn()
+    torch.cuda.synchronize()
+    if dist:
+        td.barrier()
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        dev_t, dev_st, dev_sizes = timed(dev_fn, args.steps)
+        torch.cuda.synchronize()
+        if dist:
+            td.barrier()
+        host_t, host_st, _ = timed(host_fn, args.steps)
+        torch.cuda.synchronize()
+    counters = eng.counters()
+    tot_dev = sum(dev_t)
+    tot_host = sum(host_t)
+    if dist:
+        t = torch.tensor([tot_dev, tot_host], device=f"cuda:{local}")
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        tot_dev, tot_host = t.tolist()
+    mpix = W * H / 1e6
+    value = world * args.steps * mpix / (tot_dev / 1e3)
+    e2e = world * args.steps * mpix / (tot_host / 1e3)
+
+    # stage breakdown (device-resident steps)
+    keys = dev_st[0].keys()
+    st_mean = {k: float(np.mean([s[k] for s in dev_st])) for k in keys}
+    peaks = _peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    # DWT+colour+quantisation: 5 algorithmic bytes per component-sample
+    # (1 B pixel read + 4 B int32 coefficient written).
+    dwt_bytes = 5.0 * W * H * NCOMP
+    dwt_gbs = dwt_bytes / (st_mean["dwt"] / 1e3) / 1e9 if st_mean["dwt"] > 0 else None
+    # Tier-1: 4 B per coefficient read + compressed bytes written.
+    t1_bytes = 4.0 * W * H * NCOMP + counters[3]
+    t1_gbs = t1_bytes / (st_mean["tier1"] / 1e3) / 1e9 if st_mean["tier1"] > 0 else None
+    dominant = max(("dwt", "tier1", "pcrd", "compact"), key=lambda k: st_mean[k])
+    traffic = None
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = prof.get(dominant)
+    except Exception:
+        pass
+    if dominant == "dwt":
+        roof = {"kernel": "dwt_level_kernel (all levels)", "bound": "hbm", "achieved": dwt_gbs,
+                "peak": hbm, "unit": "GB/s", "frac": dwt_gbs / hbm if dwt_gbs else None,
+                "traffic": traffic}
+    else:
+        roof = {"kernel": "t1_kernel", "bound": "hbm", "achieved": t1_gbs, "peak": hbm, "unit": "GB/s",
+                "frac": t1_gbs / hbm if t1_gbs else None, "traffic": traffic,
+                "note": "Tier-1 is issue/latency-bound (serial MQ per code-block); the HBM "
+                        "fraction shows how far it is from the bandwidth roof"}
+    roof["peak_source"] = "measured" if "fallback" not in peaks else "fallback"
+
+    line = {"metric": METRIC, "value": value, "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/i32", "data": "synthetic",
+            "config": CONFIG,
+            "latency_ms": {"p50": float(np.percentile(dev_t, 50)), "p99": float(np.percentile(dev_t, 99)),
+                           "e2e_p50": float(np.percentile(host_t, 50)),
+                           "e2e_p99": float(np.percentile(host_t, 99))},
+            "stages_ms": st_mean,
+            "e2e": {"value": e2e, "unit": "MPix/s", "h2d_bytes_per_step": W * H * NCOMP,
+                    "d2h_bytes_per_step": int(np.mean(dev_sizes))},
+            "roofline": roof,
+            "roofline_dwt": {"bound": "hbm", "achieved": dwt_gbs, "peak": hbm, "unit": "GB/s",
+                             "frac": dwt_gbs / hbm if dwt_gbs else None,
+                             "algorithmic_bytes_per_launch_set": dwt_bytes},
+            "gpu_launches": int(counters[5]) * args.steps,
+            "clocks": clocks.summary(),
+            "output_bytes": int(np.mean(dev_sizes))}
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, sec = cpu_baseline(px, 2, threads, False)
+        line["cpu_baseline"] = {"value": v, "unit": "MPix/s", "cores": threads, "kind": "port",
+                                "sample": "2 encodes of the same 2550x3300 page after 1 warm-up, "
+                                          f"{threads} threads (reference threading: components, "
+                                          "code-blocks, 9/7 rows in parallel)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

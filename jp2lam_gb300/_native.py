@@ -54,6 +54,7 @@ EXPORTS = [
 
 _lib = None
 _lock = threading.Lock()
+_engine_lock = threading.Lock()
 
 
 def load_library(path: str = LIB_PATH):
@@ -204,7 +205,7 @@ _default = None
 
 def default_engine() -> Engine:
     global _default
-    with _lock:
+    with _engine_lock:
         if _default is None:
             _default = Engine(0)
         return _default

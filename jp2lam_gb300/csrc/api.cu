@@ -60,7 +60,7 @@ struct jp2g_ctx {
   DevBuf px, ll0, ll1, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
       hulls, hulln, offsets, scratch, body;
   // pinned host staging
-  HostBuf hpx, hkeep, hoffsets, hbody;
+  HostBuf hpx, hkeep, hoffsets, hbody, hres;
   bool timing = false;
   cudaEvent_t ev[kNumStages + 1] = {};
   float stage_ms[kNumStages] = {};
@@ -363,16 +363,19 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
   // ---- compaction ----
   launch_compact(ta.blocks, pa.keep, nb, ta.out, dptr<uint8_t>(c->body), dptr<uint32_t>(c->offsets),
                  dptr<uint32_t>(c->scratch), c->stream);
-  c->counters[5] += 1 + 3 + 3;
+  c->counters[5] += 6;  // tier-1, 2 PCRD, 3 compaction kernels
   record(c, 5);
   // ---- read back ----
   if (!reserve_host(c, c->hkeep, std::max<size_t>(nb, 1) * sizeof(BlockKeep)) ||
+      !reserve_host(c, c->hres, std::max<size_t>(nb, 1) * sizeof(BlockOut)) ||
       !reserve_host(c, c->hoffsets, (size_t)(nb + 1) * 4))
     return kEncodeFailed;
   if (!cuda_ok(c, cudaMemcpyAsync(c->hkeep.p, c->keep.p, nb * sizeof(BlockKeep),
                                   cudaMemcpyDeviceToHost, c->stream), "D2H keep") ||
       !cuda_ok(c, cudaMemcpyAsync(c->hoffsets.p, c->offsets.p, (size_t)(nb + 1) * 4,
                                   cudaMemcpyDeviceToHost, c->stream), "D2H offsets") ||
+      !cuda_ok(c, cudaMemcpyAsync(c->hres.p, c->res.p, nb * sizeof(BlockOut),
+                                  cudaMemcpyDeviceToHost, c->stream), "D2H results") ||
       !cuda_ok(c, cudaStreamSynchronize(c->stream), "encode kernels"))
     return kEncodeFailed;
   const BlockKeep* hk = reinterpret_cast<const BlockKeep*>(c->hkeep.p);
@@ -402,13 +405,17 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
     cudaEventElapsedTime(&c->stage_ms[kTotal], c->ev[0], c->ev[8]);
     (void)t_host0;
   }
+  const BlockOut* hr = reinterpret_cast<const BlockOut*>(c->hres.p);
   c->counters[0] = nb;
+  for (uint32_t i = 0; i < nb; ++i) {
+    c->counters[1] += hr[i].mbp > 0;
+    c->counters[2] += hr[i].npasses;
+    c->counters[3] += hr[i].payload_len;
+    c->counters[6] += (uint64_t)hr[i].mbp * blocks[i].w * blocks[i].h;
+  }
   c->counters[4] = total;
   if (keep_out) keep_out->assign(hk, hk + nb);
-  if (res_out) {
-    res_out->resize(nb);
-    cudaMemcpy(res_out->data(), c->res.p, nb * sizeof(BlockOut), cudaMemcpyDeviceToHost);
-  }
+  if (res_out) res_out->assign(hr, hr + nb);
   if (plan_out) *plan_out = p;
   return kOk;
 }
@@ -457,7 +464,7 @@ void jp2g_destroy(jp2g_ctx* c) {
                     &c->offsets, &c->scratch, &c->body};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
-  HostBuf* hb[] = {&c->hpx, &c->hkeep, &c->hoffsets, &c->hbody};
+  HostBuf* hb[] = {&c->hpx, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres};
   for (HostBuf* b : hb)
     if (b->p) cudaFreeHost(b->p);
   for (auto& ev : c->ev)
