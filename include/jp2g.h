@@ -74,7 +74,8 @@ void* jp2g_stream(jp2g_ctx* ctx);
 /* Stage timings of the last encode, in milliseconds, measured with CUDA
  * events on the context's stream when timing is enabled:
  * [0] h2d, [1] dwt (all levels), [2] tier-1, [3] pcrd, [4] compaction,
- * [5] d2h, [6] host tier-2 + codestream, [7] total. Returns the count. */
+ * [5] d2h, [6] host tier-2 + codestream, [7] total, and the tier-1 split
+ * [8] analysis, [9] context modelling, [10] MQ coding. Returns the count. */
 int jp2g_set_timing(jp2g_ctx* ctx, int enabled);
 int jp2g_stage_times(jp2g_ctx* ctx, float* ms, int n);
 

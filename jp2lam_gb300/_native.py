@@ -159,9 +159,10 @@ class Engine:
         self.lib.jp2g_set_timing(self.handle, int(on))
 
     def stage_times(self):
-        ms = (ctypes.c_float * 8)()
-        self.lib.jp2g_stage_times(self.handle, ms, 8)
-        keys = ["h2d", "dwt", "tier1", "pcrd", "compact", "d2h", "host_t2", "total"]
+        ms = (ctypes.c_float * 11)()
+        self.lib.jp2g_stage_times(self.handle, ms, 11)
+        keys = ["h2d", "dwt", "tier1", "pcrd", "compact", "d2h", "host_t2", "total",
+                "t1_analyze", "t1_model", "t1_mq"]
         return dict(zip(keys, list(ms)))
 
     def counters(self):

@@ -45,6 +45,7 @@ struct HostBuf {
 };
 
 enum Stage { kH2D = 0, kDWT, kT1, kPCRD, kCompact, kD2H, kHost, kTotal, kNumStages };
+enum SubEvent { kEvAnalyzeEnd = kNumStages + 1, kEvModelEnd, kNumEvents };
 
 }  // namespace
 
@@ -58,12 +59,12 @@ struct jp2g_ctx {
   std::mutex mu;
   // device pools
   DevBuf px, ll0, ll1, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
-      hulls, hulln, offsets, scratch, body;
+      hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym;
   // pinned host staging
-  HostBuf hpx, hkeep, hoffsets, hbody, hres;
+  HostBuf hpx, hkeep, hoffsets, hbody, hres, hcount;
   bool timing = false;
-  cudaEvent_t ev[kNumStages + 1] = {};
-  float stage_ms[kNumStages] = {};
+  cudaEvent_t ev[kNumEvents] = {};
+  float stage_ms[kNumStages + 3] = {};
   uint64_t counters[8] = {};
 };
 
@@ -291,6 +292,8 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
       !reserve(c, c->hulln, std::max<size_t>(nb, 1)) ||
       !reserve(c, c->offsets, (size_t)(nb + 1) * 4) ||
       !reserve(c, c->scratch, ((size_t)nb / 1024 + 2) * 4) ||
+      !reserve(c, c->nplanes, std::max<size_t>(nb, 1) * 4) ||
+      !reserve(c, c->planebase, (size_t)(nb + 1) * 4) ||
       !reserve(c, c->body, std::max<size_t>(nb, 1) * slot_cap(p)))
     return kEncodeFailed;
 
@@ -342,7 +345,31 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
   ta.passes = dptr<PassRec>(c->passes);
   ta.pass_cap = pcap;
   ta.res = dptr<BlockOut>(c->res);
-  launch_t1(ta, c->num_sms, c->stream);
+  ta.nplanes = dptr<uint32_t>(c->nplanes);
+  ta.plane_base = dptr<uint32_t>(c->planebase);
+  ta.sym_slot = (uint32_t)(((size_t)p.cbw * p.cbh * 5 / 2 + 15) & ~size_t(15));
+  launch_t1_analyze(ta, c->stream);
+  launch_scan_u32(ta.nplanes, 1, nb, ta.plane_base, dptr<uint32_t>(c->scratch), c->stream);
+  // the number of (block, bit-plane) items sizes the symbol buffer
+  if (!reserve_host(c, c->hcount, 16) ||
+      !cuda_ok(c, cudaMemcpyAsync(c->hcount.p, ta.plane_base + nb, 4, cudaMemcpyDeviceToHost, c->stream),
+               "D2H item count") ||
+      !cuda_ok(c, cudaStreamSynchronize(c->stream), "tier-1 analysis"))
+    return kEncodeFailed;
+  ta.nitems = *reinterpret_cast<uint32_t*>(c->hcount.p);
+  if (!reserve(c, c->items, std::max<size_t>(ta.nitems, 1) * 4) ||
+      !reserve(c, c->itemrec, std::max<size_t>(ta.nitems, 1) * sizeof(ItemRec)) ||
+      !reserve(c, c->sym, std::max<size_t>(ta.nitems, 1) * ta.sym_slot + 64))  // reader runs 32 B ahead
+    return kEncodeFailed;
+  ta.items = dptr<uint32_t>(c->items);
+  ta.item_rec = dptr<ItemRec>(c->itemrec);
+  ta.sym = dptr<uint8_t>(c->sym);
+  launch_t1_items(ta, c->stream);
+  record(c, kEvAnalyzeEnd);
+  launch_t1_model(ta, c->num_sms, c->stream);
+  record(c, kEvModelEnd);
+  launch_t1_mq(ta, c->stream);
+  c->counters[5] += 5 + (nb > 1024 ? 1 : 0);
   record(c, 3);
   // ---- PCRD ----
   PcrdArgs pa{};
@@ -363,7 +390,7 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
   // ---- compaction ----
   launch_compact(ta.blocks, pa.keep, nb, ta.out, dptr<uint8_t>(c->body), dptr<uint32_t>(c->offsets),
                  dptr<uint32_t>(c->scratch), c->stream);
-  c->counters[5] += 6;  // tier-1, 2 PCRD, 3 compaction kernels
+  c->counters[5] += 3 + (nb > 1024 ? 1 : 0);  // 2 PCRD, scan + copy kernels
   record(c, 5);
   // ---- read back ----
   if (!reserve_host(c, c->hkeep, std::max<size_t>(nb, 1) * sizeof(BlockKeep)) ||
@@ -403,6 +430,10 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
     cudaEventSynchronize(c->ev[8]);
     for (int s = 0; s < kTotal; ++s) cudaEventElapsedTime(&c->stage_ms[s], c->ev[s], c->ev[s + 1]);
     cudaEventElapsedTime(&c->stage_ms[kTotal], c->ev[0], c->ev[8]);
+    // tier-1 split: analysis (+item list), modelling, MQ coding
+    cudaEventElapsedTime(&c->stage_ms[kNumStages + 0], c->ev[2], c->ev[kEvAnalyzeEnd]);
+    cudaEventElapsedTime(&c->stage_ms[kNumStages + 1], c->ev[kEvAnalyzeEnd], c->ev[kEvModelEnd]);
+    cudaEventElapsedTime(&c->stage_ms[kNumStages + 2], c->ev[kEvModelEnd], c->ev[3]);
     (void)t_host0;
   }
   const BlockOut* hr = reinterpret_cast<const BlockOut*>(c->hres.p);
@@ -461,10 +492,11 @@ void jp2g_destroy(jp2g_ctx* c) {
   cudaStreamSynchronize(c->stream);
   DevBuf* bufs[] = {&c->px, &c->ll0, &c->ll1, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
-                    &c->offsets, &c->scratch, &c->body};
+                    &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
+                    &c->itemrec, &c->sym};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
-  HostBuf* hb[] = {&c->hpx, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres};
+  HostBuf* hb[] = {&c->hpx, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres, &c->hcount};
   for (HostBuf* b : hb)
     if (b->p) cudaFreeHost(b->p);
   for (auto& ev : c->ev)
@@ -524,7 +556,7 @@ int jp2g_set_timing(jp2g_ctx* c, int enabled) {
 
 int jp2g_stage_times(jp2g_ctx* c, float* ms, int n) {
   if (!c || !ms) return 0;
-  int k = std::min(n, (int)kNumStages);
+  int k = std::min(n, (int)kNumStages + 3);
   for (int i = 0; i < k; ++i) ms[i] = c->stage_ms[i];
   return k;
 }

@@ -101,6 +101,17 @@ struct PassRec {
   uint16_t pad;
 };
 
+// Tier-1 modelling result of one (code-block, bit-plane) item: symbol counts
+// of its passes (SP, MR, cleanup), newly significant counts, and the number
+// of samples significant before the bit-plane.
+struct ItemRec {
+  uint32_t n_sp, n_mr, n_cl;
+  uint32_t ns_sp, ns_cl;
+  uint32_t sig_before;
+  uint32_t bitplane;
+  uint32_t pad;
+};
+
 // Tier-1 per-block result.
 struct BlockOut {
   uint32_t payload_len;  // terminated byte count (take_bytes)

@@ -44,9 +44,26 @@ struct T1Args {
   PassRec* passes;
   uint32_t pass_cap;  // pass records available per block
   BlockOut* res;
+  // (block, bit-plane) modelling items
+  uint32_t* nplanes;     // per block: magnitude bit-planes to model
+  uint32_t* plane_base;  // per block: first item (exclusive prefix of nplanes)
+  uint32_t* items;       // per item: its block
+  uint32_t nitems;
+  ItemRec* item_rec;
+  uint8_t* sym;          // per item: a slot of sym_slot symbol bytes
+  uint32_t sym_slot;
 };
 
-void launch_t1(const T1Args& a, int num_sms, cudaStream_t st);
+void launch_t1_analyze(const T1Args& a, cudaStream_t st);
+void launch_t1_items(const T1Args& a, cudaStream_t st);
+void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st);
+void launch_t1_mq(const T1Args& a, cudaStream_t st);
+
+// Exclusive prefix sum of n uint32 values read with a stride of `stride`
+// words: out[i] = sum of in[0..i), out[n] = total. `scratch` holds
+// ceil(n/1024)+1 words.
+void launch_scan_u32(const uint32_t* in, uint32_t stride, uint32_t n, uint32_t* out,
+                     uint32_t* scratch, cudaStream_t st);
 
 struct PcrdArgs {
   const BlockDesc* blocks;

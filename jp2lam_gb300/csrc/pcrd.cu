@@ -159,11 +159,11 @@ __global__ void pcrd_select_kernel(PcrdArgs a) {
 // ---------------------------------------------------------- compaction -----
 constexpr int kScanT = 1024;
 
-__global__ void scan_partial_kernel(const BlockKeep* keep, uint32_t n, uint32_t* offsets,
+__global__ void scan_partial_kernel(const uint32_t* in, uint32_t stride, uint32_t n, uint32_t* out,
                                     uint32_t* sums) {
   __shared__ uint32_t warp_tot[32];
   const uint32_t i = blockIdx.x * kScanT + threadIdx.x;
-  uint32_t v = i < n ? keep[i].body_len : 0u;
+  const uint32_t v = i < n ? in[(size_t)i * stride] : 0u;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   uint32_t x = v;
   for (int o = 1; o < 32; o <<= 1) {
@@ -181,35 +181,43 @@ __global__ void scan_partial_kernel(const BlockKeep* keep, uint32_t n, uint32_t*
     warp_tot[lane] = y;
   }
   __syncthreads();
-  uint32_t excl = x - v + (wid > 0 ? warp_tot[wid - 1] : 0u);
-  if (i < n) offsets[i] = excl;
+  const uint32_t excl = x - v + (wid > 0 ? warp_tot[wid - 1] : 0u);
+  if (i < n) out[i] = excl;
   if (threadIdx.x == kScanT - 1) sums[blockIdx.x] = excl + v;
 }
 
-__global__ void scan_sums_kernel(uint32_t* sums, uint32_t nparts, uint32_t* offsets, uint32_t n) {
-  // single thread: nparts is small (n / 1024)
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void scan_sums_kernel(uint32_t* sums, uint32_t nparts, uint32_t* out, uint32_t n) {
+  // one warp: nparts is n / 1024
+  const int lane = threadIdx.x;
   uint32_t run = 0;
-  for (uint32_t p = 0; p < nparts; ++p) {
-    uint32_t t = sums[p];
-    sums[p] = run;
-    run += t;
+  for (uint32_t p0 = 0; p0 < nparts; p0 += 32) {
+    const uint32_t p = p0 + lane;
+    const uint32_t v = p < nparts ? sums[p] : 0u;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += t;
+    }
+    if (p < nparts) sums[p] = run + x - v;
+    run += __shfl_sync(0xffffffffu, x, 31);
   }
-  offsets[n] = run;
+  if (lane == 0) out[n] = run;
+}
+
+__global__ void scan_add_kernel(uint32_t* out, uint32_t n, const uint32_t* sums) {
+  const uint32_t i = blockIdx.x * kScanT + threadIdx.x;
+  if (i < n) out[i] += sums[blockIdx.x];
 }
 
 __global__ void copy_bodies_kernel(const BlockDesc* blocks, const BlockKeep* keep, uint32_t n,
-                                   const uint8_t* src, uint8_t* dst, uint32_t* offsets,
-                                   const uint32_t* sums) {
+                                   const uint8_t* src, uint8_t* dst, const uint32_t* offsets) {
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= n) return;
-  const uint32_t off = offsets[warp] + sums[warp / kScanT];
+  const uint32_t off = offsets[warp];
   const uint32_t len = keep[warp].body_len;
   const uint8_t* s = src + blocks[warp].out_off;
   for (uint32_t i = lane; i < len; i += 32) dst[off + i] = s[i];
-  __syncwarp();
-  if (lane == 0) offsets[warp] = off;
 }
 
 }  // namespace
@@ -223,19 +231,27 @@ void launch_pcrd(const PcrdArgs& a, cudaStream_t st) {
   pcrd_select_kernel<<<g, t, 0, st>>>(a);
 }
 
+void launch_scan_u32(const uint32_t* in, uint32_t stride, uint32_t n, uint32_t* out,
+                     uint32_t* scratch, cudaStream_t st) {
+  if (n == 0) {
+    cudaMemsetAsync(out, 0, sizeof(uint32_t), st);
+    return;
+  }
+  const uint32_t parts = (n + kScanT - 1) / kScanT;
+  scan_partial_kernel<<<parts, kScanT, 0, st>>>(in, stride, n, out, scratch);
+  scan_sums_kernel<<<1, 32, 0, st>>>(scratch, parts, out, n);
+  if (parts > 1) scan_add_kernel<<<parts, kScanT, 0, st>>>(out, n, scratch);
+}
+
 void launch_compact(const BlockDesc* blocks, const BlockKeep* keep, uint32_t nblocks,
                     const uint8_t* src, uint8_t* dst, uint32_t* offsets, uint32_t* scratch,
                     cudaStream_t st) {
-  if (nblocks == 0) {
-    cudaMemsetAsync(offsets, 0, sizeof(uint32_t), st);
-    return;
-  }
-  const uint32_t parts = (nblocks + kScanT - 1) / kScanT;
-  scan_partial_kernel<<<parts, kScanT, 0, st>>>(keep, nblocks, offsets, scratch);
-  scan_sums_kernel<<<1, 32, 0, st>>>(scratch, parts, offsets, nblocks);
+  static_assert(sizeof(BlockKeep) == 12, "body_len is read as every third word");
+  launch_scan_u32(reinterpret_cast<const uint32_t*>(keep) + 1, 3, nblocks, offsets, scratch, st);
+  if (nblocks == 0) return;
   const uint32_t threads = 256;
   const uint32_t grid = (uint32_t)(((uint64_t)nblocks * 32 + threads - 1) / threads);
-  copy_bodies_kernel<<<grid, threads, 0, st>>>(blocks, keep, nblocks, src, dst, offsets, scratch);
+  copy_bodies_kernel<<<grid, threads, 0, st>>>(blocks, keep, nblocks, src, dst, offsets);
 }
 
 }  // namespace jp2g

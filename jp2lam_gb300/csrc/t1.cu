@@ -1,20 +1,31 @@
-// EBCOT Tier-1 encoder: one warp per code-block, single MQ termination per
-// block, per-pass numbytes() snapshots for rate control.
+// EBCOT Tier-1 encoder, single MQ termination per code-block, per-pass
+// numbytes() snapshots for rate control.
 //
 // Replaces analyze_codeblock (src/encode/backend/native/t1.rs:215-258) and
 // encode_codeblock_single_term (t1.rs:508-658) with its passes (SP
 // t1.rs:805-905, MR t1.rs:914-965, cleanup t1.rs:977-1197) and the MQ coder
 // (src/mq/mod.rs:163-432).
 //
-// State lives in shared memory as 64-bit row masks (bit x = column x):
-// significance and coefficient sign (with a zero row above and below),
-// visited, refined, and a window of magnitude bit-planes built once per block
-// by warp ballots. The whole warp loads the block and builds the masks; lane 0
-// then walks the passes in the reference's exact scan order (4-row stripes,
-// columns left to right, rows top to bottom) and drives the MQ coder, using
-// the masks to jump straight to the columns a pass can touch. The byte stream
-// goes directly to the block's payload slot in global memory.
+// The work is split where the dependencies allow:
+//
+// 1. t1_analyze_kernel (warp per block): max magnitude, non-zero count ->
+//    magnitude bit-planes, zero bit-planes, block class.
+// 2. t1_model_kernel (warp per (block, bit-plane)): the significance state
+//    at the start of bit-plane p is known in closed form (|q| >> (p+1) != 0),
+//    and so is the refinement history (|q| >> (p+2) != 0), so every
+//    bit-plane's three passes are modelled independently. Within a
+//    bit-plane, significance propagation is the least fixpoint of a
+//    monotone system over 64-bit row masks in which each sample only looks
+//    at samples earlier in the scan order (stripe by stripe); refinement and
+//    cleanup are then data-parallel. The warp emits the (context, bit)
+//    symbols of each stripe in exact scan order with a prefix sum over the
+//    columns (one lane per column), into a per-bit-plane symbol slot.
+// 3. t1_mq_kernel (lane per block): runs the MQ coder over a block's symbol
+//    streams, top bit-plane first, recording numbytes() after every pass
+//    and writing the byte stream to the block's payload slot.
 #include <cuda_runtime.h>
+
+#include <cstring>
 
 #include "jp2g_internal.h"
 #include "kernels.h"
@@ -23,11 +34,10 @@ namespace jp2g {
 
 namespace {
 
-constexpr int kWarps = 4;
-constexpr int kNBP = 16;  // magnitude bit-planes held in shared memory at once
-
 // Context numbers (src/mq/mod.rs:5-10).
 constexpr int kCtxAGG = 17, kCtxUNI = 18;
+constexpr int kModelWarps = 8;
+constexpr int kMqWarps = 4;
 
 struct Tables {
   uint8_t zc[4 * 512];
@@ -36,18 +46,379 @@ struct Tables {
   uint32_t mq[94];  // qe | nmps << 16 | nlps << 24
 };
 
-// Built on the host from the standard's rules and copied in at launch.
+// Built on the host from the standard's rules, copied in by upload_t1_tables.
 __constant__ Tables c_tables;
 
-struct WarpState {
-  uint64_t bp[kNBP][64];  // magnitude bit-plane window
-  uint64_t sig[68];       // row y at index y+1; rows -1 and h.. stay zero
-  uint64_t sgn[68];       // coefficient sign, same indexing
-  uint64_t vis[64];
-  uint64_t ref[64];
-  uint8_t ctx[20];
+__device__ __forceinline__ uint32_t bitat(uint64_t m, int x) { return (uint32_t)(m >> x) & 1u; }
+__device__ __forceinline__ uint64_t westm(uint64_t m) { return m << 1; }   // bit x = m[x-1]
+__device__ __forceinline__ uint64_t eastm(uint64_t m) { return m >> 1; }   // bit x = m[x+1]
+__device__ __forceinline__ uint64_t dil(uint64_t m) { return m | (m << 1) | (m >> 1); }
+
+// ---------------------------------------------------------------- analyze --
+__global__ void t1_analyze_kernel(T1Args a) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= a.nblocks) return;
+  const BlockDesc d = a.blocks[warp];
+  const int w = d.w, h = d.h;
+  const int32_t* blk = a.coef + (size_t)d.coef_slot * a.cbw * a.cbh;
+  uint32_t mx = 0, nnz = 0;
+  for (int y = 0; y < h; ++y) {
+    int32_t v0 = lane < w ? blk[y * a.cbw + lane] : 0;
+    int32_t v1 = lane + 32 < w ? blk[y * a.cbw + lane + 32] : 0;
+    uint32_t m0 = v0 < 0 ? 0u - (uint32_t)v0 : (uint32_t)v0;
+    uint32_t m1 = v1 < 0 ? 0u - (uint32_t)v1 : (uint32_t)v1;
+    mx = max(mx, max(m0, m1));
+    nnz += (v0 != 0) + (v1 != 0);
+  }
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  nnz = __reduce_add_sync(0xffffffffu, nnz);
+  if (lane != 0) return;
+  const int mbp = mx == 0 ? 0 : 32 - __clz(mx);
+  // classify_from_nonzero_fraction (src/profile.rs:122-130), in f32.
+  const float frac = __fdiv_rn((float)nnz, (float)(w * h));
+  BlockOut o{};
+  o.mbp = (uint8_t)mbp;
+  o.zbp = (uint8_t)(d.mb > mbp ? d.mb - mbp : 0);
+  o.cls = (uint8_t)(mbp == 0 ? 0 : (frac <= 0.05f ? 0 : (frac <= 0.30f ? 1 : 2)));
+  uint32_t np = mbp == 0 ? 0u : 1u + 3u * (uint32_t)(mbp - 1);
+  o.status = np > a.pass_cap ? 2 : 0;
+  o.npasses = o.status ? 0 : (uint16_t)np;
+  a.res[warp] = o;
+  a.nplanes[warp] = o.status ? 0u : (uint32_t)mbp;
+}
+
+__global__ void t1_items_kernel(T1Args a) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.nblocks) return;
+  const uint32_t base = a.plane_base[b], n = a.nplanes[b];
+  for (uint32_t j = 0; j < n; ++j) a.items[base + j] = b;
+}
+
+// ------------------------------------------------------------------ model --
+struct ModelSmem {
+  uint64_t S[68];   // significant before this bit-plane; row y at y+1
+  uint64_t N[68];   // became significant in SP; row y at y+1
+  uint64_t Q[68];   // became significant in CL; row y at y+1
+  uint64_t Sn[68];  // coefficient sign; row y at y+1
+  uint64_t B[64];   // magnitude bit p
+  uint64_t R[64];   // refinement history (|q| >> (p+2) != 0)
+  uint64_t V[64];   // visited (coded) in SP
 };
 
+struct Emitter {
+  uint64_t lo = 0, hi = 0;
+  int n = 0;
+  __device__ __forceinline__ void push(uint32_t s) {
+    hi = (hi << 8) | (lo >> 56);
+    lo = (lo << 8) | s;
+    ++n;
+  }
+  __device__ __forceinline__ uint32_t at(int i) const {  // i-th pushed symbol
+    int b = n - 1 - i;
+    return b < 8 ? (uint32_t)(lo >> (8 * b)) & 0xffu : (uint32_t)(hi >> (8 * (b - 8))) & 0xffu;
+  }
+};
+
+// Writes the lanes' symbols in lane (= column) order after `*pos`, returning
+// the symbols written.
+__device__ __forceinline__ uint32_t flush_symbols(const Emitter& e, uint8_t* out, uint32_t* pos,
+                                                  int lane) {
+  uint32_t incl = (uint32_t)e.n;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  uint8_t* dst = out + *pos + (incl - (uint32_t)e.n);
+  for (int i = 0; i < e.n; ++i) dst[i] = (uint8_t)e.at(i);
+  *pos += total;
+  return total;
+}
+
+// Sign-context index from the four cardinal neighbours' significance and
+// sign at the moment the sign is coded (src/tier1/helpers.rs:52-88).
+__device__ __forceinline__ uint32_t sign_index(uint32_t sw, uint32_t gw, uint32_t sn, uint32_t gn,
+                                               uint32_t se, uint32_t ge, uint32_t ss, uint32_t gs) {
+  return (sw << 3) | ((sw & gw) << 0) | (sn << 1) | ((sn & gn) << 4) | (se << 5) | ((se & ge) << 2) |
+         (ss << 7) | ((ss & gs) << 6);
+}
+
+struct ModelTables {
+  const uint8_t* zc;  // orientation row
+  const uint8_t* sc;
+  const uint8_t* spb;
+};
+
+// Emits a zero-coding symbol for sample (x, row) and, if it becomes
+// significant, its sign symbol. `w`, `nb` etc. are the neighbour masks as
+// seen at the sample's visit.
+__device__ __forceinline__ void emit_zc(Emitter& e, const ModelTables& t, int x, uint32_t bit,
+                                        uint64_t nwm, uint64_t nm, uint64_t nem, uint64_t wm,
+                                        uint64_t em, uint64_t swm, uint64_t sm, uint64_t sem,
+                                        uint64_t sgn_w_row, uint64_t sgn_n_row, uint64_t sgn_s_row,
+                                        uint64_t sgn_row) {
+  uint32_t m8 = bitat(nwm, x) | (bitat(nm, x) << 1) | (bitat(nem, x) << 2) | (bitat(wm, x) << 3) |
+                (bitat(em, x) << 5) | (bitat(swm, x) << 6) | (bitat(sm, x) << 7) | (bitat(sem, x) << 8);
+  e.push(((uint32_t)t.zc[m8] << 1) | bit);
+  if (bit) {
+    uint32_t sw = bitat(wm, x), sn = bitat(nm, x), se = bitat(em, x), ss = bitat(sm, x);
+    uint32_t gw = x > 0 ? bitat(sgn_w_row, x - 1) : 0u;
+    uint32_t gn = bitat(sgn_n_row, x);
+    uint32_t ge = x < 63 ? bitat(sgn_w_row, x + 1) : 0u;
+    uint32_t gs = bitat(sgn_s_row, x);
+    uint32_t lu = sign_index(sw, gw, sn, gn, se, ge, ss, gs);
+    e.push(((uint32_t)t.sc[lu] << 1) | (bitat(sgn_row, x) ^ t.spb[lu]));
+  }
+}
+
+__global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
+  __shared__ ModelSmem sm_all[kModelWarps];
+  __shared__ uint8_t s_zc[4 * 512];
+  __shared__ uint8_t s_sc[256];
+  __shared__ uint8_t s_spb[256];
+  for (int i = threadIdx.x; i < 4 * 512; i += blockDim.x) s_zc[i] = c_tables.zc[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    s_sc[i] = c_tables.sc[i];
+    s_spb[i] = c_tables.spb[i];
+  }
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  ModelSmem& s = sm_all[wid];
+  const uint32_t nwarps = gridDim.x * kModelWarps;
+
+  for (uint32_t item = blockIdx.x * kModelWarps + wid; item < a.nitems; item += nwarps) {
+    const uint32_t b = a.items[item];
+    const BlockDesc d = a.blocks[b];
+    const int w = d.w, h = d.h;
+    const int mbp = a.res[b].mbp;
+    const int j = (int)(item - a.plane_base[b]);
+    const int p = mbp - 1 - j;
+    const bool top = j == 0;
+    const uint64_t valid = w == 64 ? ~0ull : ((1ull << w) - 1);
+    const int32_t* blk = a.coef + (size_t)d.coef_slot * a.cbw * a.cbh;
+    ModelTables t{s_zc + d.orient * 512, s_sc, s_spb};
+
+    // ---- masks for this bit-plane ----
+    for (int y = 0; y < h; ++y) {
+      int32_t v0 = lane < w ? blk[y * a.cbw + lane] : 0;
+      int32_t v1 = lane + 32 < w ? blk[y * a.cbw + lane + 32] : 0;
+      uint32_t m0 = v0 < 0 ? 0u - (uint32_t)v0 : (uint32_t)v0;
+      uint32_t m1 = v1 < 0 ? 0u - (uint32_t)v1 : (uint32_t)v1;
+      uint64_t sg = (uint64_t)__ballot_sync(~0u, (m0 >> (p + 1)) != 0) |
+                    ((uint64_t)__ballot_sync(~0u, (m1 >> (p + 1)) != 0) << 32);
+      uint64_t bt = (uint64_t)__ballot_sync(~0u, (m0 >> p) & 1) |
+                    ((uint64_t)__ballot_sync(~0u, (m1 >> p) & 1) << 32);
+      uint64_t rf = (uint64_t)__ballot_sync(~0u, p + 2 < 32 && (m0 >> (p + 2)) != 0) |
+                    ((uint64_t)__ballot_sync(~0u, p + 2 < 32 && (m1 >> (p + 2)) != 0) << 32);
+      uint64_t sn = (uint64_t)__ballot_sync(~0u, v0 < 0) | ((uint64_t)__ballot_sync(~0u, v1 < 0) << 32);
+      if (lane == 0) {
+        s.S[y + 1] = sg;
+        s.B[y] = bt;
+        s.R[y] = rf;
+        s.Sn[y + 1] = sn;
+      }
+    }
+    if (lane == 0) {
+      s.S[0] = s.Sn[0] = s.N[0] = s.Q[0] = 0;
+    }
+    for (int y = h + 1 + lane; y < 68; y += 32) s.S[y] = s.Sn[y] = s.N[y] = s.Q[y] = 0;
+    __syncwarp();
+
+    uint8_t* out = a.sym + (size_t)item * a.sym_slot;
+    uint32_t pos = 0;
+    uint32_t n_sp = 0, n_mr = 0, ns_sp = 0, ns_cl = 0;
+    uint32_t sig_before = 0;
+    for (int y = lane; y < h; y += 32) sig_before += __popcll(s.S[y + 1]);
+    sig_before = __reduce_add_sync(~0u, sig_before);
+
+    if (!top) {
+      // ---- significance propagation: fixpoint per stripe ----
+      uint64_t Fp = 0;  // final SP state of the row above the stripe
+      for (int k = 0; k < h; k += 4) {
+        uint64_t S0 = s.S[k + 1], S1 = s.S[k + 2], S2 = s.S[k + 3], S3 = s.S[k + 4], D = s.S[k + 5];
+        uint64_t B0 = s.B[k], B1 = k + 1 < h ? s.B[k + 1] : 0, B2 = k + 2 < h ? s.B[k + 2] : 0,
+                 B3 = k + 3 < h ? s.B[k + 3] : 0;
+        uint64_t v0 = valid, v1 = k + 1 < h ? valid : 0, v2 = k + 2 < h ? valid : 0,
+                 v3 = k + 3 < h ? valid : 0;
+        if (k + 4 > h) D = 0;
+        uint64_t N0 = 0, N1 = 0, N2 = 0, N3 = 0, V0, V1, V2, V3;
+        for (;;) {
+          uint64_t F0 = S0 | N0, F1 = S1 | N1, F2 = S2 | N2, F3 = S3 | N3;
+          uint64_t vis0 = dil(Fp) | westm(F0) | eastm(S0) | westm(F1) | S1 | eastm(S1);
+          uint64_t vis1 = westm(F0) | F0 | eastm(S0) | westm(F1) | eastm(S1) | westm(F2) | S2 | eastm(S2);
+          uint64_t vis2 = westm(F1) | F1 | eastm(S1) | westm(F2) | eastm(S2) | westm(F3) | S3 | eastm(S3);
+          uint64_t vis3 = westm(F2) | F2 | eastm(S2) | westm(F3) | eastm(S3) | dil(D);
+          V0 = ~S0 & vis0 & v0; V1 = ~S1 & vis1 & v1; V2 = ~S2 & vis2 & v2; V3 = ~S3 & vis3 & v3;
+          uint64_t n0 = V0 & B0, n1 = V1 & B1, n2 = V2 & B2, n3 = V3 & B3;
+          if (n0 == N0 && n1 == N1 && n2 == N2 && n3 == N3) break;
+          N0 = n0; N1 = n1; N2 = n2; N3 = n3;
+        }
+        if (lane == 0) {
+          s.N[k + 1] = N0; s.N[k + 2] = N1; s.N[k + 3] = N2; s.N[k + 4] = N3;
+          s.V[k] = V0;
+          if (k + 1 < 64) s.V[k + 1] = V1;
+          if (k + 2 < 64) s.V[k + 2] = V2;
+          if (k + 3 < 64) s.V[k + 3] = V3;
+        }
+        ns_sp += __popcll(N0) + __popcll(N1) + __popcll(N2) + __popcll(N3);
+        // emission in scan order: columns are lanes, rows top to bottom
+        const uint64_t F0 = S0 | N0, F1 = S1 | N1, F2 = S2 | N2, F3 = S3 | N3;
+        const uint64_t G0 = s.Sn[k + 1], G1 = s.Sn[k + 2], G2 = s.Sn[k + 3], G3 = s.Sn[k + 4],
+                       Gp = s.Sn[k], GD = s.Sn[k + 5];
+        for (int round = 0; round * 32 < w; ++round) {
+          const int x = lane + 32 * round;
+          Emitter e;
+          if (x < w) {
+            if (bitat(V0, x))
+              emit_zc(e, t, x, bitat(B0, x), westm(Fp), Fp, eastm(Fp), westm(F0), eastm(S0), westm(F1), S1,
+                      eastm(S1), G0, Gp, G1, G0);
+            if (bitat(V1, x))
+              emit_zc(e, t, x, bitat(B1, x), westm(F0), F0, eastm(S0), westm(F1), eastm(S1), westm(F2), S2,
+                      eastm(S2), G1, G0, G2, G1);
+            if (bitat(V2, x))
+              emit_zc(e, t, x, bitat(B2, x), westm(F1), F1, eastm(S1), westm(F2), eastm(S2), westm(F3), S3,
+                      eastm(S3), G2, G1, G3, G2);
+            if (bitat(V3, x))
+              emit_zc(e, t, x, bitat(B3, x), westm(F2), F2, eastm(S2), westm(F3), eastm(S3), westm(D), D,
+                      eastm(D), G3, G2, GD, G3);
+          }
+          n_sp += flush_symbols(e, out, &pos, lane);
+        }
+        Fp = F3;
+        if (k + 4 > h) break;
+      }
+      __syncwarp();
+      // ---- magnitude refinement ----
+      for (int k = 0; k < h; k += 4) {
+        const int lim = min(4, h - k);
+        for (int round = 0; round * 32 < w; ++round) {
+          const int x = lane + 32 * round;
+          Emitter e;
+          if (x < w) {
+            for (int r = 0; r < lim; ++r) {
+              const int y = k + r;
+              const uint64_t Sy = s.S[y + 1];
+              if (!bitat(Sy, x)) continue;
+              const uint64_t Gu = s.S[y] | s.N[y], Gm = Sy | s.N[y + 1], Gd = s.S[y + 2] | s.N[y + 2];
+              uint32_t nb = bitat(dil(Gu) | westm(Gm) | eastm(Gm) | dil(Gd), x);
+              uint32_t cx = bitat(s.R[y], x) ? 16u : (nb ? 15u : 14u);  // helpers.rs:36-50
+              e.push((cx << 1) | bitat(s.B[y], x));
+            }
+          }
+          n_mr += flush_symbols(e, out, &pos, lane);
+        }
+      }
+    } else {
+      for (int y = lane; y < 64; y += 32) s.V[y] = 0;
+      for (int y = lane; y < 68; y += 32) s.N[y] = 0;
+      __syncwarp();
+    }
+
+    // ---- cleanup ----
+    {
+      uint64_t Gp = 0;  // final state (after this cleanup) of the row above
+      const uint32_t start = pos;
+      for (int k = 0; k < h; k += 4) {
+        const int lim = min(4, h - k);
+        uint64_t Gr[4], Vr[4], Br[4], Cr[4], Qr[4], Fr[4], Sg[4];
+        for (int r = 0; r < 4; ++r) {
+          const bool in = r < lim;
+          Gr[r] = in ? (s.S[k + r + 1] | s.N[k + r + 1]) : 0;
+          Vr[r] = in ? s.V[k + r] : 0;
+          Br[r] = in ? s.B[k + r] : 0;
+          Sg[r] = s.Sn[k + r + 1];
+          Cr[r] = in ? (~Gr[r] & ~Vr[r] & valid) : 0;
+          Qr[r] = Cr[r] & Br[r];
+          Fr[r] = Gr[r] | Qr[r];
+        }
+        const uint64_t Gd = lim == 4 && k + 4 < h ? (s.S[k + 5] | s.N[k + 5]) : 0;  // next stripe, pre-CL
+        const uint64_t SgP = s.Sn[k], SgD = s.Sn[k + 5];
+        ns_cl += __popcll(Qr[0]) + __popcll(Qr[1]) + __popcll(Qr[2]) + __popcll(Qr[3]);
+        if (lane == 0)
+          for (int r = 0; r < lim; ++r) s.Q[k + r + 1] = Qr[r];
+        // run-length eligibility of each column (flags.rs:219-235)
+        uint64_t clean = 0;
+        if (lim == 4) {
+          uint64_t busy = Gr[0] | Gr[1] | Gr[2] | Gr[3] | Vr[0] | Vr[1] | Vr[2] | Vr[3];
+          uint64_t nbr = dil(Gp) | westm(Fr[0] | Fr[1] | Fr[2] | Fr[3]) |
+                         eastm(Gr[0] | Gr[1] | Gr[2] | Gr[3]) | dil(Gd);
+          clean = ~(busy | nbr) & valid;
+        }
+        for (int round = 0; round * 32 < w; ++round) {
+          const int x = lane + 32 * round;
+          Emitter e;
+          if (x < w) {
+            int first = 0;
+            if (bitat(clean, x)) {
+              uint32_t nib = bitat(Br[0], x) | (bitat(Br[1], x) << 1) | (bitat(Br[2], x) << 2) |
+                             (bitat(Br[3], x) << 3);
+              if (nib == 0) {
+                e.push((uint32_t)kCtxAGG << 1);
+                first = 4;
+              } else {
+                const int rl = __ffs(nib) - 1;
+                e.push(((uint32_t)kCtxAGG << 1) | 1u);
+                e.push(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl >> 1));
+                e.push(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl & 1u));
+                // sign of the run's first significant sample
+                const uint64_t Nm = rl == 0 ? Gp : Fr[rl - 1];
+                const uint64_t Sm = rl < 3 ? Gr[rl + 1] : Gd;
+                uint32_t sw = bitat(westm(Fr[rl]), x), sn = bitat(Nm, x);
+                uint32_t se = bitat(eastm(Gr[rl]), x), ss = bitat(Sm, x);
+                uint32_t gw = x > 0 ? bitat(Sg[rl], x - 1) : 0u;
+                uint32_t gn = bitat(rl == 0 ? SgP : Sg[rl - 1], x);
+                uint32_t ge = x < 63 ? bitat(Sg[rl], x + 1) : 0u;
+                uint32_t gs = bitat(rl < 3 ? Sg[rl + 1] : SgD, x);
+                uint32_t lu = sign_index(sw, gw, sn, gn, se, ge, ss, gs);
+                e.push(((uint32_t)t.sc[lu] << 1) | (bitat(Sg[rl], x) ^ t.spb[lu]));
+                first = rl + 1;
+              }
+            }
+            for (int r = first; r < lim; ++r) {
+              if (!bitat(Cr[r], x)) continue;
+              const uint64_t Nr = r == 0 ? Gp : Fr[r - 1];
+              const uint64_t NEr = r == 0 ? Gp : Gr[r - 1];
+              const uint64_t Dr = r < 3 ? Gr[r + 1] : Gd;
+              const uint64_t DWr = r < 3 ? Fr[r + 1] : Gd;
+              emit_zc(e, t, x, bitat(Br[r], x), westm(Nr), Nr, eastm(NEr), westm(Fr[r]), eastm(Gr[r]),
+                      westm(DWr), Dr, eastm(Dr), Sg[r], r == 0 ? SgP : Sg[r - 1], r < 3 ? Sg[r + 1] : SgD,
+                      Sg[r]);
+            }
+          }
+          flush_symbols(e, out, &pos, lane);
+        }
+        Gp = Fr[lim - 1];
+      }
+      if (lane == 0) {
+        ItemRec rec;
+        rec.n_sp = n_sp;
+        rec.n_mr = n_mr;
+        rec.n_cl = pos - start;
+        rec.ns_sp = ns_sp;
+        rec.ns_cl = ns_cl;
+        rec.sig_before = sig_before;
+        rec.bitplane = (uint32_t)p;
+        rec.pad = 0;
+        a.item_rec[item] = rec;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// --------------------------------------------------------------------- MQ --
+// The coder runs one code-block per lane. Every step is written without
+// data-dependent branches (conditional exchange, renormalisation and byte
+// output are predicated), so the 32 lanes of a warp, each coding a different
+// block, stay converged; only pass boundaries and stream refills branch.
+//
+// Per context the shared table holds the full probability-state entry
+// (qe | MPS << 16 | next-MPS index << 17 | next-LPS index << 24), so one load
+// yields qe and the MPS; the state table T is only consulted to move a
+// context to its next state.
 struct Mq {
   uint32_t a, c, ct;
   int pos;        // index of the last written byte; 0 is the pre-byte
@@ -57,72 +428,55 @@ struct Mq {
   int ovf;
 };
 
-__device__ __forceinline__ void mq_emit(Mq& m, uint32_t b) {
+// BYTEOUT (src/mq/mod.rs:382-404) as straight-line code: a carry into the
+// previous byte is applied first, then one byte is emitted (7 bits after an
+// 0xFF, 8 otherwise).
+__device__ __forceinline__ void mq_byteout(Mq& m) {
+  const bool carry = m.last != 0xffu && (m.c & 0x8000000u) != 0;
+  if (carry) {
+    m.last = (m.last + 1) & 0xffu;
+    if (m.pos >= 1 && m.pos <= m.cap) m.out[m.pos - 1] = (uint8_t)m.last;
+    if (m.last == 0xffu) m.c &= 0x7ffffffu;
+  }
+  const bool big = m.last == 0xffu;
+  const uint32_t byte = (big ? (m.c >> 20) : (m.c >> 19)) & 0xffu;
+  m.c &= big ? 0xfffffu : 0x7ffffu;
+  m.ct = big ? 7u : 8u;
   ++m.pos;
-  m.last = b & 0xffu;
-  if (m.pos <= m.cap) m.out[m.pos - 1] = (uint8_t)m.last;
+  m.last = byte;
+  if (m.pos <= m.cap) m.out[m.pos - 1] = (uint8_t)byte;
   else m.ovf = 1;
 }
 
-// BYTEOUT with carry propagation and 0xFF bit stuffing (src/mq/mod.rs:382-404).
-__device__ __forceinline__ void mq_byteout(Mq& m) {
-  if (m.last == 0xffu) {
-    mq_emit(m, m.c >> 20);
-    m.c &= 0xfffffu;
-    m.ct = 7;
-  } else if ((m.c & 0x8000000u) == 0) {
-    mq_emit(m, m.c >> 19);
-    m.c &= 0x7ffffu;
-    m.ct = 8;
-  } else {
-    m.last = (m.last + 1) & 0xffu;
-    if (m.pos >= 1 && m.pos <= m.cap) m.out[m.pos - 1] = (uint8_t)m.last;
-    if (m.last == 0xffu) {
-      m.c &= 0x7ffffffu;
-      mq_emit(m, m.c >> 20);
-      m.c &= 0xfffffu;
-      m.ct = 7;
-    } else {
-      mq_emit(m, m.c >> 19);
-      m.c &= 0x7ffffu;
-      m.ct = 8;
+// One MQ symbol. `e` is the context's current state entry; returns the
+// entry the context holds afterwards.
+__device__ __forceinline__ uint32_t mq_step(Mq& m, uint32_t e, uint32_t bit, const uint32_t* T) {
+  const uint32_t qe = e & 0xffffu;
+  const bool is_mps = bit == ((e >> 16) & 1u);
+  const uint32_t a = m.a - qe;
+  const bool ren = !is_mps || (a & 0x8000u) == 0;
+  const bool lt = a < qe;
+  // conditional exchange (C.2.5, C.2.6)
+  const bool add_c = is_mps ? (!ren || !lt) : lt;
+  const bool take_qe = is_mps ? (ren && lt) : !lt;
+  m.c += add_c ? qe : 0u;
+  uint32_t na = take_qe ? qe : a;
+  uint32_t ne = e;
+  if (ren) ne = T[is_mps ? ((e >> 17) & 0x7fu) : (e >> 24)];
+  // RENORME in one step; at most three bytes come out
+  uint32_t n = __clz(na) - 16;
+  m.a = na << n;
+  #pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    if (n >= m.ct) {
+      m.c <<= m.ct;
+      n -= m.ct;
+      mq_byteout(m);
     }
-  }
-}
-
-// RENORME: shift until A >= 0x8000, emitting a byte whenever CT runs out.
-__device__ __forceinline__ void mq_renorm(Mq& m) {
-  uint32_t n = __clz(m.a) - 16;
-  m.a <<= n;
-  while (n >= m.ct) {
-    m.c <<= m.ct;
-    n -= m.ct;
-    mq_byteout(m);
   }
   m.c <<= n;
   m.ct -= n;
-}
-
-__device__ __forceinline__ void mq_encode(Mq& m, uint8_t* ctx, int cx, uint32_t bit) {
-  uint32_t st = ctx[cx];
-  uint32_t e = c_tables.mq[st];
-  uint32_t qe = e & 0xffffu;
-  m.a -= qe;
-  if (bit == (st & 1u)) {
-    if ((m.a & 0x8000u) == 0) {
-      if (m.a < qe) m.a = qe;
-      else m.c += qe;
-      ctx[cx] = (uint8_t)((e >> 16) & 0xff);
-      mq_renorm(m);
-    } else {
-      m.c += qe;
-    }
-  } else {
-    if (m.a < qe) m.c += qe;
-    else m.a = qe;
-    ctx[cx] = (uint8_t)(e >> 24);
-    mq_renorm(m);
-  }
+  return ne;
 }
 
 __device__ __forceinline__ void mq_flush(Mq& m) {  // src/mq/mod.rs:244-250, 373-379
@@ -135,289 +489,92 @@ __device__ __forceinline__ void mq_flush(Mq& m) {  // src/mq/mod.rs:244-250, 373
   mq_byteout(m);
 }
 
-__device__ __forceinline__ uint32_t win3(uint64_t r, int x) {
-  return x == 0 ? (uint32_t)((r << 1) & 7u) : (uint32_t)((r >> (x - 1)) & 7u);
-}
-
-// Neighbour significance mask (NW N NE W . E SW S SE -> bits 0..8).
-__device__ __forceinline__ uint32_t nmask(const uint64_t* S, int x, int y) {
-  return win3(S[y], x) | ((win3(S[y + 1], x) & 5u) << 3) | (win3(S[y + 2], x) << 6);
-}
-
-// Sign-context index from the four cardinal neighbours
-// (src/tier1/helpers.rs:52-88, src/tier1/flags.rs:237-296).
-__device__ __forceinline__ uint32_t sign_lu(const uint64_t* S, const uint64_t* G, int x, int y) {
-  uint32_t lu = 0;
-  uint64_t mid = S[y + 1], gm = G[y + 1];
-  if (x > 0 && ((mid >> (x - 1)) & 1)) lu |= 8u | (uint32_t)((gm >> (x - 1)) & 1);
-  if ((S[y] >> x) & 1) lu |= 2u | ((uint32_t)((G[y] >> x) & 1) << 4);
-  if (x < 63 && ((mid >> (x + 1)) & 1)) lu |= 32u | ((uint32_t)((gm >> (x + 1)) & 1) << 2);
-  if ((S[y + 2] >> x) & 1) lu |= 128u | ((uint32_t)((G[y + 2] >> x) & 1) << 6);
-  return lu;
-}
-
-struct Block {
-  int w, h;
-  uint64_t valid;
-  const uint8_t* zc;
+// Reads a bit-plane's symbol stream 16 bytes at a time; the next chunk is
+// requested before the current one is consumed.
+struct SymReader {
+  const uint4* p;
+  uint4 cur, nxt;
+  int k;  // symbols left in `cur`
+  __device__ __forceinline__ void start(const uint8_t* base) {
+    p = reinterpret_cast<const uint4*>(base);
+    cur = p[0];
+    nxt = p[1];
+    p += 2;
+    k = 16;
+  }
+  __device__ __forceinline__ uint32_t next() {
+    if (k == 0) {
+      cur = nxt;
+      nxt = *p++;
+      k = 16;
+    }
+    const int i = 16 - k;
+    const uint32_t w = i < 4 ? cur.x : (i < 8 ? cur.y : (i < 12 ? cur.z : cur.w));
+    --k;
+    return (w >> (8 * (i & 3))) & 0xffu;
+  }
 };
 
-// Codes the sign of a sample that just became significant and marks it.
-__device__ __forceinline__ void code_sign(Mq& m, WarpState& ws, int x, int y) {
-  uint32_t lu = sign_lu(ws.sig, ws.sgn, x, y);
-  uint32_t s = (uint32_t)((ws.sgn[y + 1] >> x) & 1);
-  mq_encode(m, ws.ctx, c_tables.sc[lu], s ^ c_tables.spb[lu]);
-  ws.sig[y + 1] |= 1ull << x;
-}
-
-// Significance propagation (t1.rs:805-905).
-__device__ uint32_t sig_pass(Mq& m, WarpState& ws, const Block& b, const uint64_t* bpm) {
-  uint32_t ns = 0;
-  uint64_t* S = ws.sig;
-  for (int k = 0; k < b.h; k += 4) {
-    const int lim = min(4, b.h - k);
-    int x = 0;
-    while (x < b.w) {
-      uint64_t any = 0, all = ~0ull;
-      for (int r = 0; r < lim + 2; ++r) any |= S[k + r];
-      for (int r = 0; r < lim; ++r) all &= S[k + 1 + r];
-      uint64_t cand = (any | (any << 1) | (any >> 1)) & ~all & b.valid & (~0ull << x);
-      if (cand == 0) break;
-      x = __ffsll((long long)cand) - 1;
-      const uint64_t bx = 1ull << x;
-      for (int ci = 0; ci < lim; ++ci) {
-        const int y = k + ci;
-        if (S[y + 1] & bx) continue;
-        uint32_t nm = nmask(S, x, y);
-        if (nm == 0) continue;
-        uint32_t bit = (uint32_t)((bpm[y] >> x) & 1);
-        mq_encode(m, ws.ctx, b.zc[nm], bit);
-        ws.vis[y] |= bx;
-        if (bit) {
-          code_sign(m, ws, x, y);
-          ++ns;
-        }
-      }
-      ++x;
-    }
+__global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a) {
+  __shared__ uint32_t T[94];
+  __shared__ uint32_t ce_all[kMqWarps][20 * 32];
+  for (int i = threadIdx.x; i < 94; i += blockDim.x) {
+    // expand (qe | nmps << 16 | nlps << 24) to (qe | mps << 16 | nmps << 17 | nlps << 24)
+    const uint32_t v = c_tables.mq[i];
+    T[i] = (v & 0xffffu) | ((uint32_t)(i & 1) << 16) | (((v >> 16) & 0x7fu) << 17) | ((v >> 24) << 24);
   }
-  return ns;
-}
-
-// Magnitude refinement (t1.rs:914-965).
-__device__ void ref_pass(Mq& m, WarpState& ws, const Block& b, const uint64_t* bpm) {
-  uint64_t* S = ws.sig;
-  for (int k = 0; k < b.h; k += 4) {
-    const int lim = min(4, b.h - k);
-    uint64_t col = 0;
-    for (int ci = 0; ci < lim; ++ci) col |= S[k + ci + 1] & ~ws.vis[k + ci];
-    while (col) {
-      const int x = __ffsll((long long)col) - 1;
-      col &= col - 1;
-      const uint64_t bx = 1ull << x;
-      for (int ci = 0; ci < lim; ++ci) {
-        const int y = k + ci;
-        if (!(S[y + 1] & ~ws.vis[y] & bx)) continue;
-        int cx = (ws.ref[y] & bx) ? 16 : (nmask(S, x, y) ? 15 : 14);  // helpers.rs:36-50
-        mq_encode(m, ws.ctx, cx, (uint32_t)((bpm[y] >> x) & 1));
-        ws.ref[y] |= bx;
-      }
-    }
-  }
-}
-
-// Regular (non run-length) cleanup step; returns true if the sample became
-// significant (t1.rs:1150-1197).
-__device__ __forceinline__ bool cl_sample(Mq& m, WarpState& ws, const Block& b,
-                                          const uint64_t* bpm, int x, int y) {
-  const uint64_t bx = 1ull << x;
-  if ((ws.sig[y + 1] | ws.vis[y]) & bx) return false;
-  uint32_t nm = nmask(ws.sig, x, y);
-  uint32_t bit = (uint32_t)((bpm[y] >> x) & 1);
-  mq_encode(m, ws.ctx, nm ? b.zc[nm] : 0, bit);
-  if (bit) code_sign(m, ws, x, y);
-  return bit != 0;
-}
-
-// Columns of a full stripe that qualify for run-length coding: no sample
-// significant or visited, no significant neighbour (flags.rs:219-235).
-__device__ __forceinline__ uint64_t clean_cols(const WarpState& ws, int k, uint64_t valid) {
-  uint64_t sv = 0, any = 0;
-  for (int ci = 0; ci < 4; ++ci) sv |= ws.sig[k + ci + 1] | ws.vis[k + ci];
-  for (int r = 0; r < 6; ++r) any |= ws.sig[k + r];
-  return ~(sv | any | (any << 1) | (any >> 1)) & valid;
-}
-
-// Cleanup pass (t1.rs:977-1148).
-__device__ uint32_t cleanup_pass(Mq& m, WarpState& ws, const Block& b, const uint64_t* bpm) {
-  uint32_t ns = 0;
-  const int full = b.h & ~3;
-  for (int k = 0; k < full; k += 4) {
-    uint64_t clean = clean_cols(ws, k, b.valid);
-    for (int x = 0; x < b.w; ++x) {
-      const uint64_t bx = 1ull << x;
-      if (clean & bx) {
-        uint32_t nib = (uint32_t)((bpm[k] >> x) & 1) | ((uint32_t)((bpm[k + 1] >> x) & 1) << 1) |
-                       ((uint32_t)((bpm[k + 2] >> x) & 1) << 2) | ((uint32_t)((bpm[k + 3] >> x) & 1) << 3);
-        if (nib == 0) {
-          mq_encode(m, ws.ctx, kCtxAGG, 0);
-          continue;
-        }
-        const int rl = __ffs(nib) - 1;
-        mq_encode(m, ws.ctx, kCtxAGG, 1);
-        mq_encode(m, ws.ctx, kCtxUNI, (uint32_t)(rl >> 1) & 1);
-        mq_encode(m, ws.ctx, kCtxUNI, (uint32_t)rl & 1);
-        code_sign(m, ws, x, k + rl);
-        ++ns;
-        for (int ci = rl + 1; ci < 4; ++ci) ns += cl_sample(m, ws, b, bpm, x, k + ci);
-        clean = clean_cols(ws, k, b.valid);
-      } else {
-        bool changed = false;
-        for (int ci = 0; ci < 4; ++ci) {
-          bool s = cl_sample(m, ws, b, bpm, x, k + ci);
-          ns += s;
-          changed |= s;
-        }
-        if (changed) clean = clean_cols(ws, k, b.valid);
-      }
-    }
-  }
-  if (full < b.h) {  // partial stripe: never run-length coded
-    const int lim = b.h - full;
-    for (int x = 0; x < b.w; ++x)
-      for (int ci = 0; ci < lim; ++ci) ns += cl_sample(m, ws, b, bpm, x, full + ci);
-  }
-  for (int y = 0; y < b.h; ++y) ws.vis[y] = 0;  // clear_visited_all
-  return ns;
-}
-
-// Builds bit-planes [base, base+kNBP) of the block's magnitudes, one ballot
-// per row half.
-__device__ void build_planes(WarpState& ws, const int32_t* blk, int cbw, int w, int h, int base,
-                             int top, int lane) {
-  for (int y = 0; y < h; ++y) {
-    int32_t v0 = lane < w ? blk[y * cbw + lane] : 0;
-    int32_t v1 = lane + 32 < w ? blk[y * cbw + lane + 32] : 0;
-    uint32_t m0 = v0 < 0 ? (uint32_t)(-(int64_t)v0) : (uint32_t)v0;
-    uint32_t m1 = v1 < 0 ? (uint32_t)(-(int64_t)v1) : (uint32_t)v1;
-    for (int p = base; p < top && p < base + kNBP; ++p) {
-      uint32_t lo = __ballot_sync(0xffffffffu, (m0 >> p) & 1);
-      uint32_t hi = __ballot_sync(0xffffffffu, (m1 >> p) & 1);
-      if (lane == 0) ws.bp[p - base][y] = (uint64_t)lo | ((uint64_t)hi << 32);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(kWarps * 32) t1_kernel(T1Args a) {
-  __shared__ WarpState states[kWarps];
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
-  WarpState& ws = states[wid];
-  const uint32_t gwarp = blockIdx.x * kWarps + wid;
-  const uint32_t nwarps = gridDim.x * kWarps;
+  uint32_t* ce = &ce_all[wid][lane];  // context c at ce[32 * c]
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.nblocks) return;
+  BlockOut o = a.res[b];
+  const int mbp = o.status ? 0 : o.mbp;
+  if (mbp == 0) return;
+  const BlockDesc d = a.blocks[b];
+  // contexts: state 0 except UNI 46, AGG 3, ZC 4 (src/mq/mod.rs:195-200)
+  for (int c = 0; c < 19; ++c) ce[32 * c] = T[0];
+  ce[32 * kCtxUNI] = T[92];
+  ce[32 * kCtxAGG] = T[6];
+  ce[0] = T[8];
+  Mq m{0x8000u, 0u, 12u, 0, 0u, a.out + d.out_off, (int)d.out_cap, 0};
+  PassRec* pr = a.passes + d.pass_off;
+  const uint32_t base = a.plane_base[b];
 
-  for (uint32_t bi = gwarp; bi < a.nblocks; bi += nwarps) {
-    const BlockDesc d = a.blocks[bi];
-    const int w = d.w, h = d.h;
-    const int32_t* blk = a.coef + (size_t)d.coef_slot * a.cbw * a.cbh;
-
-    // ---- analysis: max magnitude, non-zero count, signs ----
-    uint32_t mx = 0, nnz = 0;
-    for (int y = 0; y < h; ++y) {
-      int32_t v0 = lane < w ? blk[y * a.cbw + lane] : 0;
-      int32_t v1 = lane + 32 < w ? blk[y * a.cbw + lane + 32] : 0;
-      uint32_t m0 = v0 < 0 ? (uint32_t)(-(int64_t)v0) : (uint32_t)v0;
-      uint32_t m1 = v1 < 0 ? (uint32_t)(-(int64_t)v1) : (uint32_t)v1;
-      mx = max(mx, max(m0, m1));
-      nnz += __popc(__ballot_sync(0xffffffffu, v0 != 0)) + __popc(__ballot_sync(0xffffffffu, v1 != 0));
-      uint32_t s0 = __ballot_sync(0xffffffffu, v0 < 0), s1 = __ballot_sync(0xffffffffu, v1 < 0);
-      if (lane == 0) ws.sgn[y + 1] = (uint64_t)s0 | ((uint64_t)s1 << 32);
-    }
-    mx = __reduce_max_sync(0xffffffffu, mx);
-    const int mbp = mx == 0 ? 0 : 32 - __clz(mx);
-    const int zbp = d.mb > mbp ? d.mb - mbp : 0;
-    // classify_from_nonzero_fraction (src/profile.rs:122-130), in f32.
-    const float frac = __fdiv_rn((float)nnz, (float)(w * h));
-    const int cls = mbp == 0 ? 0 : (frac <= 0.05f ? 0 : (frac <= 0.30f ? 1 : 2));
-    const uint32_t npasses = mbp == 0 ? 0u : 1u + 3u * (uint32_t)(mbp - 1);
-
-    if (mbp == 0 || npasses > a.pass_cap) {
-      if (lane == 0) {
-        BlockOut o{};
-        o.payload_len = 0;
-        o.npasses = 0;
-        o.mbp = (uint8_t)mbp;
-        o.zbp = (uint8_t)zbp;
-        o.cls = (uint8_t)cls;
-        o.status = mbp == 0 ? 0 : 2;
-        a.res[bi] = o;
+  // pass walk: item j (bit-plane mbp-1-j), pass k (top item: cleanup only)
+  int j = 0, k = 2, pi = 0;
+  ItemRec r = a.item_rec[base];
+  SymReader rd;
+  rd.start(a.sym + (size_t)base * a.sym_slot);
+  uint32_t left = r.n_cl;
+  for (;;) {
+    while (left == 0) {  // end of a pass: snapshot numbytes(), move on
+      const uint8_t bp = (uint8_t)r.bitplane;
+      if (k == 0) pr[pi++] = PassRec{(uint32_t)m.pos, r.ns_sp, r.sig_before, 0, bp, 0};
+      else if (k == 1) pr[pi++] = PassRec{(uint32_t)m.pos, 0u, r.sig_before, 1, bp, 0};
+      else pr[pi++] = PassRec{(uint32_t)m.pos, r.ns_cl, j == 0 ? 0u : r.sig_before + r.ns_sp, 2, bp, 0};
+      if (k < 2) {
+        ++k;
+        left = k == 1 ? r.n_mr : r.n_cl;
+        continue;
       }
-      __syncwarp();
-      continue;
+      if (++j == mbp) break;
+      r = a.item_rec[base + j];
+      rd.start(a.sym + (size_t)(base + j) * a.sym_slot);
+      k = 0;
+      left = r.n_sp;
     }
-
-    // ---- state init ----
-    for (int i = lane; i < 68; i += 32) ws.sig[i] = 0;
-    if (lane == 0) { ws.sgn[0] = 0; }
-    for (int i = h + 1 + lane; i < 68; i += 32) ws.sgn[i] = 0;
-    for (int i = lane; i < 64; i += 32) { ws.vis[i] = 0; ws.ref[i] = 0; }
-    if (lane < 20) ws.ctx[lane] = 0;
-    __syncwarp();
-    if (lane == 0) {  // src/mq/mod.rs:195-200
-      ws.ctx[kCtxUNI] = 92;
-      ws.ctx[kCtxAGG] = 6;
-      ws.ctx[0] = 8;
-    }
-    int base = mbp > kNBP ? mbp - kNBP : 0;
-    build_planes(ws, blk, a.cbw, w, h, base, mbp, lane);
-    __syncwarp();
-
-    Mq m{0x8000u, 0u, 12u, 0, 0u, a.out + d.out_off, (int)d.out_cap, 0};
-    Block b{w, h, w == 64 ? ~0ull : ((1ull << w) - 1), c_tables.zc + d.orient * 512};
-    PassRec* pr = a.passes + d.pass_off;
-    uint32_t sig_so_far = 0;
-    int pi = 0;
-
-    for (int p = mbp - 1; p >= 0; --p) {
-      if (p < base) {
-        base = p + 1 > kNBP ? p + 1 - kNBP : 0;
-        build_planes(ws, blk, a.cbw, w, h, base, p + 1, lane);
-        __syncwarp();
-      }
-      if (lane == 0) {
-        const uint64_t* bpm = ws.bp[p - base];
-        if (p == mbp - 1) {
-          uint32_t ns = cleanup_pass(m, ws, b, bpm);
-          pr[pi++] = PassRec{(uint32_t)m.pos, ns, 0u, 2, (uint8_t)p, 0};
-          sig_so_far += ns;
-        } else {
-          const uint32_t before = sig_so_far;
-          uint32_t sp = sig_pass(m, ws, b, bpm);
-          pr[pi++] = PassRec{(uint32_t)m.pos, sp, before, 0, (uint8_t)p, 0};
-          sig_so_far += sp;
-          ref_pass(m, ws, b, bpm);
-          pr[pi++] = PassRec{(uint32_t)m.pos, 0u, before, 1, (uint8_t)p, 0};
-          uint32_t cl = cleanup_pass(m, ws, b, bpm);
-          pr[pi++] = PassRec{(uint32_t)m.pos, cl, sig_so_far, 2, (uint8_t)p, 0};
-          sig_so_far += cl;
-        }
-      }
-      __syncwarp();
-    }
-
-    if (lane == 0) {
-      mq_flush(m);
-      BlockOut o{};
-      o.payload_len = (uint32_t)(m.last == 0xffu ? m.pos - 1 : m.pos);  // take_bytes
-      o.npasses = (uint16_t)npasses;
-      o.mbp = (uint8_t)mbp;
-      o.zbp = (uint8_t)zbp;
-      o.cls = (uint8_t)cls;
-      o.status = m.ovf ? 1 : 0;
-      a.res[bi] = o;
-    }
-    __syncwarp();
+    if (j == mbp) break;
+    const uint32_t sym = rd.next();
+    const uint32_t cx = sym >> 1;
+    ce[32 * cx] = mq_step(m, ce[32 * cx], sym & 1u, T);
+    --left;
   }
+  mq_flush(m);
+  o.payload_len = (uint32_t)(m.last == 0xffu ? m.pos - 1 : m.pos);  // take_bytes
+  o.status = m.ovf ? 1 : 0;
+  a.res[b] = o;
 }
 
 }  // namespace
@@ -432,13 +589,29 @@ bool upload_t1_tables(const uint8_t* zc, const uint8_t* sc, const uint8_t* spb,
   return cudaMemcpyToSymbol(c_tables, &t, sizeof t) == cudaSuccess;
 }
 
-void launch_t1(const T1Args& a, int num_sms, cudaStream_t st) {
+void launch_t1_analyze(const T1Args& a, cudaStream_t st) {
   if (a.nblocks == 0) return;
-  uint32_t need = (a.nblocks + kWarps - 1) / kWarps;
-  uint32_t grid = need;
-  uint32_t cap = (uint32_t)num_sms * 16;  // persistent: several CTAs per SM
-  if (grid > cap) grid = cap;
-  t1_kernel<<<grid, kWarps * 32, 0, st>>>(a);
+  const uint32_t threads = 256;
+  const uint32_t grid = (uint32_t)(((uint64_t)a.nblocks * 32 + threads - 1) / threads);
+  t1_analyze_kernel<<<grid, threads, 0, st>>>(a);
+}
+
+void launch_t1_items(const T1Args& a, cudaStream_t st) {
+  if (a.nblocks == 0) return;
+  t1_items_kernel<<<(a.nblocks + 255) / 256, 256, 0, st>>>(a);
+}
+
+void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st) {
+  if (a.nitems == 0) return;
+  uint32_t need = (a.nitems + kModelWarps - 1) / kModelWarps;
+  uint32_t cap = (uint32_t)num_sms * 8;
+  t1_model_kernel<<<need < cap ? need : cap, kModelWarps * 32, 0, st>>>(a);
+}
+
+void launch_t1_mq(const T1Args& a, cudaStream_t st) {
+  if (a.nblocks == 0) return;
+  const uint32_t threads = kMqWarps * 32;
+  t1_mq_kernel<<<(a.nblocks + threads - 1) / threads, threads, 0, st>>>(a);
 }
 
 }  // namespace jp2g
