@@ -3,8 +3,8 @@
  *
  * The drop-in boundary for jp2lam's encode path. A Rust (or any FFI) host
  * keeps jp2lam's public types (Image, EncodeOptions, BatchEncoder) and calls
- * these entry points instead of NativeBackend; see INTEGRATION.md for the
- * extern "C" binding. Plain pointers and sizes only.
+ * these entry points instead of NativeBackend through an extern "C" block.
+ * Plain pointers and sizes only.
  *
  * Status codes map 1:1 to jp2lam::Jp2LamError (src/error.rs:7-13):
  *   0 ok, 1 InvalidInput, 2 EncodeFailed, 3 DecodeFailed,
