@@ -96,6 +96,35 @@ int jp2g_debug_blocks(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,
                       uint32_t ncomp, uint8_t quality, int32_t* rows, uint32_t cap,
                       uint32_t* nblocks);
 
+/* Allocation-free first stage of the encoder: level shift + RCT/ICT, every
+ * DWT level and the deadzone quantiser, for callers that cannot allocate
+ * device memory -- code recorded into a CUDA graph, plug-in hosts that only
+ * lend pre-allocated buffers, and real-time loops that must not call the
+ * allocator (cudaMalloc can synchronise the whole device). It has no
+ * counterpart in the reference, whose encoder always allocates.
+ *
+ * d_px: interleaved 8-bit pixels in device memory (w * h * ncomp bytes).
+ * d_coef: device buffer of w * h * ncomp int32 that receives the quantised
+ * coefficients (the reversible coefficients at quality 100) of each
+ * component as a w x h plane in subband (Mallat) layout, component after
+ * component -- the same values the full encoder codes.
+ * stream: a cudaStream_t (NULL = the legacy default stream). The call only
+ * enqueues kernels; synchronise the stream before reading d_coef.
+ *
+ * The call allocates nothing: its scratch (the intermediate LL planes) is
+ * one statically sized 8 MiB device array that every GPU loading this
+ * library holds until the process exits. Limit: ceil(w/2) * ceil(h/2) *
+ * ncomp <= 1048576 whenever the image gets two or more decomposition levels
+ * (e.g. 2048x2048 gray or 1182x1182 RGB); larger images are rejected with
+ * JP2G_INVALID_INPUT and a message before any device work. All calls share
+ * the array, so calls that overlap on the GPU (other streams or threads on
+ * the same device) race and must be serialised by the caller. The first call
+ * on a device looks up the array's device address for that device; make it
+ * before any stream capture. On failure jp2g_last_error(NULL) holds the
+ * message. */
+int jp2g_dwt_noalloc(const uint8_t* d_px, uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality,
+                     int32_t* d_coef, void* stream);
+
 /* Host-only, no device needed: the Tier-1 context tables (zero coding
  * 4x512, sign context 256, sign prediction 256) and the MQ state table
  * (94 entries, qe | next_mps << 16 | next_lps << 24) the kernels use. */

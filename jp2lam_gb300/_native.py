@@ -49,7 +49,7 @@ _BY_CODE = {1: InvalidInput, 2: EncodeFailed, 3: DecodeFailed, 4: UnsupportedFea
 EXPORTS = [
     "jp2g_create", "jp2g_destroy", "jp2g_encode", "jp2g_encode_device", "jp2g_free",
     "jp2g_last_error", "jp2g_stream", "jp2g_set_timing", "jp2g_stage_times", "jp2g_counters",
-    "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_tables",
+    "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
 ]
 
 _lib = None
@@ -90,6 +90,8 @@ def load_library(path: str = LIB_PATH):
                                           ctypes.c_void_p, ctypes.c_uint32,
                                           ctypes.POINTER(ctypes.c_uint32)]
         lib.jp2g_tables.argtypes = [ctypes.c_void_p] * 4
+        lib.jp2g_dwt_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.c_uint8, ctypes.c_void_p, ctypes.c_void_p]
         _lib = lib
         return lib
 

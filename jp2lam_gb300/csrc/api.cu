@@ -453,6 +453,11 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
 
 }  // namespace
 
+namespace jp2g {
+// Records a message for jp2g_last_error(NULL) on the calling thread.
+void set_thread_error(const char* msg) { g_create_error = msg ? msg : ""; }
+}  // namespace jp2g
+
 extern "C" {
 
 int jp2g_create(jp2g_ctx** out, int device, uint64_t hbm_budget_bytes) {

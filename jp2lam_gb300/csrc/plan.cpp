@@ -192,3 +192,56 @@ bool build_plan(uint32_t w, uint32_t h, int ncomp, int quality, int format,
 }
 
 }  // namespace jp2g
+
+namespace jp2g {
+
+// Allocation-free subset of build_plan for the DWT stage: decomposition
+// levels, the reversible flag, the f32 quantiser step of every band (LL, then
+// HL/LH/HH per resolution) and the resolution ladder (rw/rh: size of
+// resolution r; lo_w/lo_h: size of resolution r-1, i.e. of the LL band that
+// resolution r's level produces). Arrays hold up to 1 + 3*6 steps and 7
+// resolutions.
+bool plan_dwt_steps(uint32_t w, uint32_t h, int ncomp, int quality, int* levels, int* lossless,
+                    float* steps, int* lo_w, int* lo_h, int* rw, int* rh) {
+  if (w == 0 || h == 0 || (ncomp != 1 && ncomp != 3) || quality < 0 || quality > 255) return false;
+  const bool rev = quality >= 100;
+  const int L = std::min(decompositions(w, h), ncomp == 3 ? 6 : 5);
+  const int nres = L + 1;
+  const int precision = 8;
+  const double scale = rev ? 1.0 : step_scaler(quality);
+  int k = 0;
+  for (int r = 0; r <= L; ++r)
+    for (int oi = 0; oi < (r == 0 ? 1 : 3); ++oi) {
+      const int o = r == 0 ? LL : oi + 1;
+      int e, m = 0;
+      if (rev) {
+        e = precision + band_gain(o);
+      } else {
+        int level = std::max(std::max(nres - 1, 0) - r, 0);
+        double st = (double)(1u << band_gain(o)) / norm97(level, o);
+        pack_step((int)std::floor(st * 8192.0), precision + band_gain(o), &e, &m);
+        rescale(scale, &e, &m);
+      }
+      float base = 1.0f + (float)m / 2048.0f;
+      float s = base * std::ldexp(1.0f, precision + band_gain(o) - e);
+      steps[k++] = s > 1e-6f ? s : 1e-6f;
+    }
+  int cw[8], chh[8];
+  cw[L] = (int)w;
+  chh[L] = (int)h;
+  for (int r = L - 1; r >= 0; --r) {
+    cw[r] = (cw[r + 1] + 1) / 2;
+    chh[r] = (chh[r + 1] + 1) / 2;
+  }
+  for (int r = 0; r <= L; ++r) {
+    rw[r] = cw[r];
+    rh[r] = chh[r];
+    lo_w[r] = r > 0 ? cw[r - 1] : 0;
+    lo_h[r] = r > 0 ? chh[r - 1] : 0;
+  }
+  *levels = L;
+  *lossless = rev ? 1 : 0;
+  return true;
+}
+
+}  // namespace jp2g
