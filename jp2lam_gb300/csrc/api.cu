@@ -359,7 +359,7 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
   ta.nitems = *reinterpret_cast<uint32_t*>(c->hcount.p);
   if (!reserve(c, c->items, std::max<size_t>(ta.nitems, 1) * 4) ||
       !reserve(c, c->itemrec, std::max<size_t>(ta.nitems, 1) * sizeof(ItemRec)) ||
-      !reserve(c, c->sym, std::max<size_t>(ta.nitems, 1) * ta.sym_slot + 64))  // reader runs 32 B ahead
+      !reserve(c, c->sym, std::max<size_t>(ta.nitems, 1) * ta.sym_slot + 64))  // the MQ reader runs 48 B ahead
     return kEncodeFailed;
   ta.items = dptr<uint32_t>(c->items);
   ta.item_rec = dptr<ItemRec>(c->itemrec);
@@ -368,7 +368,7 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
   record(c, kEvAnalyzeEnd);
   launch_t1_model(ta, c->num_sms, c->stream);
   record(c, kEvModelEnd);
-  launch_t1_mq(ta, c->stream);
+  launch_t1_mq(ta, c->num_sms, c->stream);
   c->counters[5] += 5 + (nb > 1024 ? 1 : 0);
   record(c, 3);
   // ---- PCRD ----

@@ -448,31 +448,29 @@ __device__ __forceinline__ void mq_byteout(Mq& m) {
   else m.ovf = 1;
 }
 
-// One MQ symbol. `e` is the context's current state entry; returns the
-// entry the context holds afterwards.
+// One MQ symbol (C.2.4-C.2.7). `e` is the context's state entry; returns the
+// entry the context holds afterwards. The exchange is predicated; the only
+// branch is the rare one that emits bytes.
 __device__ __forceinline__ uint32_t mq_step(Mq& m, uint32_t e, uint32_t bit, const uint32_t* T) {
   const uint32_t qe = e & 0xffffu;
   const bool is_mps = bit == ((e >> 16) & 1u);
   const uint32_t a = m.a - qe;
   const bool ren = !is_mps || (a & 0x8000u) == 0;
   const bool lt = a < qe;
-  // conditional exchange (C.2.5, C.2.6)
   const bool add_c = is_mps ? (!ren || !lt) : lt;
   const bool take_qe = is_mps ? (ren && lt) : !lt;
   m.c += add_c ? qe : 0u;
-  uint32_t na = take_qe ? qe : a;
+  const uint32_t na = take_qe ? qe : a;
   uint32_t ne = e;
   if (ren) ne = T[is_mps ? ((e >> 17) & 0x7fu) : (e >> 24)];
-  // RENORME in one step; at most three bytes come out
-  uint32_t n = __clz(na) - 16;
+  uint32_t n = __clz(na) - 16;  // RENORME in one step
   m.a = na << n;
-  #pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    if (n >= m.ct) {
+  if (n >= m.ct) {
+    do {
       m.c <<= m.ct;
       n -= m.ct;
       mq_byteout(m);
-    }
+    } while (n >= m.ct);
   }
   m.c <<= n;
   m.ct -= n;
@@ -489,33 +487,47 @@ __device__ __forceinline__ void mq_flush(Mq& m) {  // src/mq/mod.rs:244-250, 373
   mq_byteout(m);
 }
 
-// Reads a bit-plane's symbol stream 16 bytes at a time; the next chunk is
-// requested before the current one is consumed.
-struct SymReader {
-  const uint4* p;
-  uint4 cur, nxt;
-  int k;  // symbols left in `cur`
-  __device__ __forceinline__ void start(const uint8_t* base) {
-    p = reinterpret_cast<const uint4*>(base);
-    cur = p[0];
-    nxt = p[1];
-    p += 2;
-    k = 16;
-  }
-  __device__ __forceinline__ uint32_t next() {
-    if (k == 0) {
-      cur = nxt;
-      nxt = *p++;
-      k = 16;
-    }
-    const int i = 16 - k;
-    const uint32_t w = i < 4 ? cur.x : (i < 8 ? cur.y : (i < 12 ? cur.z : cur.w));
-    --k;
-    return (w >> (8 * (i & 3))) & 0xffu;
-  }
-};
+// Symbol i (0..15) of a 16-byte chunk.
+__device__ __forceinline__ uint32_t chunk_sym(const uint4& q, int i) {
+  const uint32_t w = i < 8 ? (i < 4 ? q.x : q.y) : (i < 12 ? q.z : q.w);
+  return (w >> (8 * (i & 3))) & 0xffu;
+}
 
-__global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a) {
+// Codes all 16 symbols of a chunk, the next symbol's context entry loaded
+// one step ahead of its use.
+__device__ __forceinline__ void mq_chunk16(Mq& m, uint32_t* ce, const uint32_t* T, const uint4 q) {
+  uint32_t sym = q.x & 0xffu;
+  uint32_t e = ce[32 * (sym >> 1)];
+  #pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const uint32_t symn = i < 15 ? chunk_sym(q, i + 1) : 0u;
+    const uint32_t cx = sym >> 1, cxn = symn >> 1;
+    uint32_t en = i < 15 ? ce[32 * cxn] : 0u;
+    const uint32_t ne = mq_step(m, e, sym & 1u, T);
+    ce[32 * cx] = ne;
+    if (cxn == cx) en = ne;
+    e = en;
+    sym = symn;
+  }
+}
+
+// Codes symbols [from, to) of a chunk one at a time (chunks that hold a pass
+// end or the end of the stream).
+__device__ __forceinline__ void mq_chunk_part(Mq& m, uint32_t* ce, const uint32_t* T, const uint4 q,
+                                              int from, int to) {
+  for (int i = from; i < to; ++i) {
+    const uint32_t sym = chunk_sym(q, i);
+    const uint32_t cx = sym >> 1;
+    ce[32 * cx] = mq_step(m, ce[32 * cx], sym & 1u, T);
+  }
+}
+
+// Per-block MQ coding over the symbol streams of the block's bit-planes.
+// Blocks go `bpw` to a warp, one per lane: 32 when enough blocks are in
+// flight to fill the GPU, 1 when a single page leaves it mostly idle and the
+// longest block's serial chain sets the time (lanes of a warp diverge on
+// every byte emitted, which lengthens each lane's chain).
+__global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw) {
   __shared__ uint32_t T[94];
   __shared__ uint32_t ce_all[kMqWarps][20 * 32];
   for (int i = threadIdx.x; i < 94; i += blockDim.x) {
@@ -526,8 +538,9 @@ __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a) {
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
+  if (lane >= bpw) return;
   uint32_t* ce = &ce_all[wid][lane];  // context c at ce[32 * c]
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t b = (blockIdx.x * kMqWarps + wid) * (uint32_t)bpw + (uint32_t)lane;
   if (b >= a.nblocks) return;
   BlockOut o = a.res[b];
   const int mbp = o.status ? 0 : o.mbp;
@@ -541,35 +554,51 @@ __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a) {
   Mq m{0x8000u, 0u, 12u, 0, 0u, a.out + d.out_off, (int)d.out_cap, 0};
   PassRec* pr = a.passes + d.pass_off;
   const uint32_t base = a.plane_base[b];
-
-  // pass walk: item j (bit-plane mbp-1-j), pass k (top item: cleanup only)
-  int j = 0, k = 2, pi = 0;
-  ItemRec r = a.item_rec[base];
-  SymReader rd;
-  rd.start(a.sym + (size_t)base * a.sym_slot);
-  uint32_t left = r.n_cl;
-  for (;;) {
-    while (left == 0) {  // end of a pass: snapshot numbytes(), move on
-      const uint8_t bp = (uint8_t)r.bitplane;
-      if (k == 0) pr[pi++] = PassRec{(uint32_t)m.pos, r.ns_sp, r.sig_before, 0, bp, 0};
-      else if (k == 1) pr[pi++] = PassRec{(uint32_t)m.pos, 0u, r.sig_before, 1, bp, 0};
-      else pr[pi++] = PassRec{(uint32_t)m.pos, r.ns_cl, j == 0 ? 0u : r.sig_before + r.ns_sp, 2, bp, 0};
-      if (k < 2) {
-        ++k;
-        left = k == 1 ? r.n_mr : r.n_cl;
+  int pi = 0;
+  for (int j = 0; j < mbp; ++j) {
+    // item j codes bit-plane mbp-1-j: SP | MR | CL, or CL alone for j = 0
+    const ItemRec r = a.item_rec[base + j];
+    const uint8_t bp = (uint8_t)r.bitplane;
+    const int total = (int)(r.n_sp + r.n_mr + r.n_cl);
+    const int npass = j == 0 ? 1 : 3;
+    int end[3];  // symbol index at which each pass ends
+    end[0] = j == 0 ? total : (int)r.n_sp;
+    end[1] = (int)(r.n_sp + r.n_mr);
+    end[2] = total;
+    auto snapshot = [&](int k) {  // numbytes() after pass k
+      if (npass == 1 || k == 2)
+        pr[pi++] = PassRec{(uint32_t)m.pos, r.ns_cl, j == 0 ? 0u : r.sig_before + r.ns_sp, 2, bp, 0};
+      else if (k == 0)
+        pr[pi++] = PassRec{(uint32_t)m.pos, r.ns_sp, r.sig_before, 0, bp, 0};
+      else
+        pr[pi++] = PassRec{(uint32_t)m.pos, 0u, r.sig_before, 1, bp, 0};
+    };
+    int k = 0;  // next pass to close
+    while (k < npass - 1 && end[k] == 0) snapshot(k++);
+    const uint4* src = reinterpret_cast<const uint4*>(a.sym + (size_t)(base + j) * a.sym_slot);
+    const int nch = (total + 15) >> 4;
+    uint4 c0 = src[0], c1 = src[1], c2 = src[2];
+    for (int ch = 0; ch < nch; ++ch) {
+      const uint4 cur = c0;
+      c0 = c1;
+      c1 = c2;
+      c2 = src[ch + 3];  // 48 bytes ahead: inside the slot or the buffer's 64-byte pad
+      const int lo = ch << 4, hi = lo + 16;
+      if (hi <= total && (k == npass - 1 || end[k] >= hi)) {
+        mq_chunk16(m, ce, T, cur);  // no pass ends inside the chunk
+      } else {
+        const int lim = min(hi, total);
+        for (int at = lo; at < lim;) {
+          const int stop = k == npass - 1 ? lim : min(lim, end[k]);
+          mq_chunk_part(m, ce, T, cur, at - lo, stop - lo);
+          at = stop;
+          while (k < npass - 1 && end[k] == at) snapshot(k++);
+        }
         continue;
       }
-      if (++j == mbp) break;
-      r = a.item_rec[base + j];
-      rd.start(a.sym + (size_t)(base + j) * a.sym_slot);
-      k = 0;
-      left = r.n_sp;
+      while (k < npass - 1 && end[k] == hi) snapshot(k++);
     }
-    if (j == mbp) break;
-    const uint32_t sym = rd.next();
-    const uint32_t cx = sym >> 1;
-    ce[32 * cx] = mq_step(m, ce[32 * cx], sym & 1u, T);
-    --left;
+    snapshot(npass == 1 ? 0 : 2);
   }
   mq_flush(m);
   o.payload_len = (uint32_t)(m.last == 0xffu ? m.pos - 1 : m.pos);  // take_bytes
@@ -608,10 +637,13 @@ void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st) {
   t1_model_kernel<<<need < cap ? need : cap, kModelWarps * 32, 0, st>>>(a);
 }
 
-void launch_t1_mq(const T1Args& a, cudaStream_t st) {
+void launch_t1_mq(const T1Args& a, int num_sms, cudaStream_t st) {
   if (a.nblocks == 0) return;
-  const uint32_t threads = kMqWarps * 32;
-  t1_mq_kernel<<<(a.nblocks + threads - 1) / threads, threads, 0, st>>>(a);
+  // One block per warp while that keeps at most 48 warps per SM; 32 per warp
+  // beyond that.
+  const int bpw = a.nblocks <= (uint32_t)num_sms * 48u ? 1 : 32;
+  const uint32_t per_cta = (uint32_t)bpw * kMqWarps;
+  t1_mq_kernel<<<(a.nblocks + per_cta - 1) / per_cta, kMqWarps * 32, 0, st>>>(a, bpw);
 }
 
 }  // namespace jp2g
