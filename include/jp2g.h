@@ -31,7 +31,8 @@ enum {
   JP2G_ENCODE_FAILED = 2,
   JP2G_DECODE_FAILED = 3,
   JP2G_UNSUPPORTED_FEATURE = 4,
-  JP2G_IO = 5
+  JP2G_IO = 5,
+  JP2G_PENDING = 6 /* jp2g_poll only: the result is not ready yet */
 };
 
 enum { JP2G_FORMAT_J2K = 0, JP2G_FORMAT_JP2 = 1 };
@@ -62,6 +63,62 @@ int jp2g_encode_device(jp2g_ctx* ctx, const uint8_t* d_px, uint32_t w, uint32_t 
                        size_t* out_len);
 
 void jp2g_free(uint8_t* p);
+
+/* One page of a batch or a served request. `px` holds w*h*ncomp 8-bit
+ * samples: host memory, or device memory of the context's GPU when
+ * on_device != 0 (then interleaved). Gray is ncomp 1; sRGB is ncomp 3,
+ * interleaved RGBRGB (interleaved != 0, Image::from_rgb_bytes) or planar.
+ * quality 0..255 (>= 100 is lossless, as EncodeOptions::quality);
+ * format 0 = J2K, 1 = JP2. */
+typedef struct jp2g_request {
+  const uint8_t* px;
+  uint32_t width, height, ncomp;
+  int32_t interleaved;
+  int32_t on_device;
+  int32_t quality;
+  int32_t format;
+} jp2g_request;
+
+/* Encodes n pages. Pages are grouped into device waves that share one flat
+ * code-block work list (colour+DWT per page, then Tier-1, PCRD and
+ * compaction over all the wave's blocks in single launches); the host
+ * Tier-2 of one wave overlaps the next wave's device work. Per page:
+ * outs[i]/out_lens[i] receive the codestream (free with jp2g_free) and
+ * status[i] its status; one page's failure does not fail the others.
+ * Returns JP2G_OK, or the first failing page's status (its message in
+ * jp2g_last_error). Output bytes equal jp2g_encode's for each page.
+ * Replaces BatchEncoder::encode_one / encode_all and encode_batch
+ * (src/batch.rs:39-70, 173), which encode page after page. */
+int jp2g_encode_batch(jp2g_ctx* ctx, const jp2g_request* reqs, uint32_t n, uint8_t** outs,
+                      size_t* out_lens, int* status);
+
+/* Continuous batching. jp2g_submit validates the request (validate_image,
+ * src/plan/validate.rs:4-62, before any device work) and queues it; a
+ * worker thread admits queued requests into the next device wave as the
+ * previous one leaves the device, up to JP2G_OPT_WAVE_BLOCKS code-blocks,
+ * while a second thread writes the codestreams of finished waves. The pixel
+ * buffer must stay valid until jp2g_poll has returned the ticket's result.
+ * jp2g_poll waits up to timeout_ms (< 0: no limit) and returns the
+ * request's status with its codestream, or JP2G_PENDING if it is not done
+ * (poll again); a returned result releases the ticket. Both calls are
+ * thread-safe. No reference counterpart: the reference has no server
+ * loop. */
+int jp2g_submit(jp2g_ctx* ctx, const jp2g_request* req, uint64_t* ticket);
+int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, int timeout_ms);
+
+/* Tuning knobs (the autotuner sets these):
+ * JP2G_OPT_WAVE_BLOCKS        most code-blocks per device wave (default 160000);
+ * JP2G_OPT_MQ_BLOCKS_PER_WARP code-blocks per warp in MQ coding, 1..32, or 0
+ *                             for automatic (1 for small work lists, else 32);
+ * JP2G_OPT_HOST_THREADS       host threads for staging and Tier-2 (0 = all). */
+enum {
+  JP2G_OPT_WAVE_BLOCKS = 0,
+  JP2G_OPT_MQ_BLOCKS_PER_WARP = 1,
+  JP2G_OPT_HOST_THREADS = 2,
+  JP2G_NUM_OPTS = 3
+};
+int jp2g_set_option(jp2g_ctx* ctx, int option, int64_t value);
+int jp2g_get_option(jp2g_ctx* ctx, int option, int64_t* value);
 
 /* Message of the last failed call on this context (or of the last failed
  * jp2g_create when ctx is NULL). */

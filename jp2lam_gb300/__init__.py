@@ -26,7 +26,7 @@ from ._native import Engine, Jp2LamError, InvalidInput, EncodeFailed, DecodeFail
 __all__ = [
     "ColorSpace", "OutputFormat", "Preset", "Image", "Component", "EncodeOptions",
     "encode", "encode_to_writer", "BatchEncoder", "BatchProfile", "encode_batch",
-    "Engine", "Jp2LamError", "InvalidInput", "EncodeFailed", "DecodeFailed",
+    "encode_pages", "Server", "Engine", "Jp2LamError", "InvalidInput", "EncodeFailed", "DecodeFailed",
     "UnsupportedFeature", "IoError",
 ]
 
@@ -195,8 +195,61 @@ class BatchEncoder:
         return out
 
     def encode_all(self, images: Iterable[Image]) -> List[bytes]:
-        return [self.encode_one(im) for im in images]
+        """Same results as encode_one on each image in turn, but the pages go
+        to the device together (jp2g_encode_batch). As in the reference, a
+        profile mismatch at item k fails the call after items 0..k-1."""
+        images = list(images)
+        bad = None
+        for k, im in enumerate(images):
+            try:
+                _validate(im)
+                self._validate_or_set_profile(im)
+            except Jp2LamError as err:
+                bad = (k, err)
+                break
+        good = images if bad is None else images[:bad[0]]
+        outs = encode_pages([(im, self.options) for im in good], self._engine)
+        self._count += len(outs)
+        if bad is not None:
+            raise bad[1]
+        return outs
 
 
 def encode_batch(images: Iterable[Image], options: EncodeOptions) -> List[bytes]:
     return BatchEncoder(options).encode_all(images)
+
+
+def _page(image: Image, options: EncodeOptions) -> dict:
+    return {"px": image.data, "w": image.width, "h": image.height, "ncomp": image.ncomp,
+            "quality": int(options.quality), "fmt": int(options.format)}
+
+
+def encode_pages(items, engine: Optional[Engine] = None) -> List[bytes]:
+    """Encodes (Image, EncodeOptions) pairs of any sizes, colours and
+    qualities in device waves; each result equals encode(image, options).
+    Raises the first failing page's error."""
+    items = list(items)
+    for im, _ in items:
+        _validate(im)
+    eng = engine or default_engine()
+    outs = eng.encode_batch([_page(im, op) for im, op in items])
+    for o in outs:
+        if isinstance(o, Exception):
+            raise o
+    return outs
+
+
+class Server:
+    """Continuous batching over jp2g_submit / jp2g_poll: pages submitted while
+    others are on the device join the next device wave."""
+
+    def __init__(self, engine: Optional[Engine] = None):
+        self.engine = engine or default_engine()
+
+    def submit(self, image: Image, options: Optional[EncodeOptions] = None) -> int:
+        _validate(image)
+        return self.engine.submit(_page(image, options or EncodeOptions()))
+
+    def result(self, ticket: int, timeout_ms: int = -1) -> Optional[bytes]:
+        """The codestream, or None if not ready within timeout_ms."""
+        return self.engine.poll(ticket, timeout_ms)

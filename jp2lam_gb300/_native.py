@@ -50,7 +50,20 @@ EXPORTS = [
     "jp2g_create", "jp2g_destroy", "jp2g_encode", "jp2g_encode_device", "jp2g_free",
     "jp2g_last_error", "jp2g_stream", "jp2g_set_timing", "jp2g_stage_times", "jp2g_counters",
     "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
+    "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
 ]
+
+PENDING = 6
+OPT_WAVE_BLOCKS = 0
+OPT_MQ_BLOCKS_PER_WARP = 1
+OPT_HOST_THREADS = 2
+
+
+class Request(ctypes.Structure):
+    """jp2g_request: one page of a batch or a served request."""
+    _fields_ = [("px", ctypes.c_void_p), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("ncomp", ctypes.c_uint32), ("interleaved", ctypes.c_int32), ("on_device", ctypes.c_int32),
+                ("quality", ctypes.c_int32), ("format", ctypes.c_int32)]
 
 _lib = None
 _lock = threading.Lock()
@@ -92,6 +105,14 @@ def load_library(path: str = LIB_PATH):
         lib.jp2g_tables.argtypes = [ctypes.c_void_p] * 4
         lib.jp2g_dwt_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                          ctypes.c_uint8, ctypes.c_void_p, ctypes.c_void_p]
+        lib.jp2g_encode_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_uint32,
+                                          ctypes.POINTER(_u8p), ctypes.POINTER(ctypes.c_size_t),
+                                          ctypes.POINTER(ctypes.c_int)]
+        lib.jp2g_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]
+        lib.jp2g_poll.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(_u8p),
+                                  ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]
+        lib.jp2g_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
+        lib.jp2g_get_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
         _lib = lib
         return lib
 
@@ -111,6 +132,8 @@ class Engine:
             _raise(rc, self.lib.jp2g_last_error(None).decode())
         self.handle = h
         self._lock = threading.Lock()
+        self._inflight = {}  # ticket -> pixel buffer kept alive until polled
+        self._inflight_lock = threading.Lock()
 
     def close(self):
         if getattr(self, "handle", None):
@@ -153,6 +176,82 @@ class Engine:
         data = ctypes.string_at(out, n.value)
         self.lib.jp2g_free(out)
         return data
+
+    @staticmethod
+    def _request(page, keep):
+        """Builds a Request from a dict with px (host array/bytes or device
+        pointer int with on_device=True), w, h, ncomp, quality, fmt and
+        optionally interleaved."""
+        on_dev = bool(page.get("on_device", False))
+        w, h, nc = int(page["w"]), int(page["h"]), int(page["ncomp"])
+        if on_dev:
+            ptr = int(page["px"])
+        else:
+            px = page["px"]
+            buf = np.frombuffer(px, dtype=np.uint8) if isinstance(px, (bytes, bytearray)) else \
+                np.ascontiguousarray(px, dtype=np.uint8)
+            if buf.size != w * h * nc:
+                raise InvalidInput("pixel buffer length does not match the image dimensions")
+            keep.append(buf)
+            ptr = buf.ctypes.data
+        return Request(ptr, w, h, nc, int(page.get("interleaved", True)), int(on_dev),
+                       int(page["quality"]), int(page["fmt"]))
+
+    def encode_batch(self, pages):
+        """Encodes a list of page dicts in device waves. Returns a list with
+        the codestream bytes of each page, or the exception its status maps
+        to."""
+        keep = []
+        n = len(pages)
+        reqs = (Request * max(n, 1))(*[self._request(p, keep) for p in pages])
+        outs = (_u8p * max(n, 1))()
+        lens = (ctypes.c_size_t * max(n, 1))()
+        status = (ctypes.c_int * max(n, 1))()
+        with self._lock:
+            rc = self.lib.jp2g_encode_batch(self.handle, reqs, n, outs, lens, status)
+            msg = self.lib.jp2g_last_error(self.handle).decode() if rc != 0 else ""
+        result = []
+        for i in range(n):
+            if status[i] == 0:
+                result.append(ctypes.string_at(outs[i], lens[i]))
+                self.lib.jp2g_free(outs[i])
+            else:
+                result.append(_BY_CODE.get(status[i], Jp2LamError)(msg or f"page {i} failed"))
+        return result
+
+    def submit(self, page) -> int:
+        """Queues one page dict for continuous batching; returns its ticket."""
+        keep = []
+        req = self._request(page, keep)
+        t = ctypes.c_uint64()
+        rc = self.lib.jp2g_submit(self.handle, ctypes.byref(req), ctypes.byref(t))
+        self._check(rc)
+        with self._inflight_lock:
+            self._inflight[t.value] = keep
+        return t.value
+
+    def poll(self, ticket: int, timeout_ms: int = -1):
+        """The ticket's codestream, or None if it is not done within
+        timeout_ms. Raises the page's error if it failed."""
+        out = _u8p()
+        n = ctypes.c_size_t()
+        rc = self.lib.jp2g_poll(self.handle, ticket, ctypes.byref(out), ctypes.byref(n), timeout_ms)
+        if rc == PENDING:
+            return None
+        with self._inflight_lock:
+            self._inflight.pop(ticket, None)
+        self._check(rc)
+        data = ctypes.string_at(out, n.value)
+        self.lib.jp2g_free(out)
+        return data
+
+    def set_option(self, option: int, value: int):
+        self._check(self.lib.jp2g_set_option(self.handle, option, value))
+
+    def get_option(self, option: int) -> int:
+        v = ctypes.c_int64()
+        self._check(self.lib.jp2g_get_option(self.handle, option, ctypes.byref(v)))
+        return v.value
 
     def stream(self) -> int:
         return self.lib.jp2g_stream(self.handle)

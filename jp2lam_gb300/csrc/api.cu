@@ -9,11 +9,17 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/jp2g.h"
@@ -47,6 +53,31 @@ struct HostBuf {
 enum Stage { kH2D = 0, kDWT, kT1, kPCRD, kCompact, kD2H, kHost, kTotal, kNumStages };
 enum SubEvent { kEvAnalyzeEnd = kNumStages + 1, kEvModelEnd, kNumEvents };
 
+// One page of a wave: its request, its plan and, after the device phase,
+// the page-local retained blocks and bytes that Tier-2 needs.
+struct PageJob {
+  const uint8_t* host_px = nullptr;
+  const uint8_t* dev_px = nullptr;
+  uint32_t w = 0, h = 0, ncomp = 0;
+  int interleaved = 1, quality = 0, format = 0;
+  int status = 0;
+  std::string err;
+  PagePlan plan;            // band first_block relative to the page
+  uint32_t block_base = 0;  // the page's first code-block in the wave
+  size_t px_off = 0;        // the page's pixels in the wave's staging buffer
+  std::vector<BlockKeep> keep;
+  std::vector<uint32_t> offsets;  // nblocks + 1 body offsets
+  std::vector<uint8_t> body;
+  std::vector<uint8_t> out;       // the codestream (J2K or JP2)
+};
+
+// A submitted request and, once done, its result.
+struct Ticket {
+  uint64_t id = 0;
+  PageJob job;
+  bool done = false;
+};
+
 }  // namespace
 
 struct jp2g_ctx {
@@ -66,6 +97,18 @@ struct jp2g_ctx {
   cudaEvent_t ev[kNumEvents] = {};
   float stage_ms[kNumStages + 3] = {};
   uint64_t counters[8] = {};
+  int64_t opt[JP2G_NUM_OPTS] = {160000, 0, 0};
+  // submit/poll: a worker thread forms waves from the queue and runs their
+  // device phase; a finisher thread runs Tier-2 of finished waves, so the
+  // next wave's device work overlaps the previous wave's host work.
+  std::mutex qmu;
+  std::condition_variable qcv, fcv, dcv;
+  std::deque<std::shared_ptr<Ticket>> pending;
+  std::deque<std::vector<std::shared_ptr<Ticket>>> finishing;
+  std::unordered_map<uint64_t, std::shared_ptr<Ticket>> tickets;
+  uint64_t next_ticket = 1;
+  bool stop = false;
+  std::thread worker, finisher;
 };
 
 namespace {
@@ -126,15 +169,17 @@ uint32_t pass_cap(const PagePlan& p) {
   return (uint32_t)(1 + 3 * (maxbp - 1));
 }
 
-// Host-side work list, band and component tables for one page.
-void build_tables(const PagePlan& p, std::vector<BlockDesc>* blocks, std::vector<BandParam>* bands,
-                  std::vector<CompParam>* comps) {
-  const uint32_t cap = slot_cap(p), pcap = pass_cap(p);
-  blocks->resize(p.nblocks);
+// Appends one page's code-blocks, PCRD band constants and component keys to
+// the wave's tables; the page's blocks start at `block_base`, its band
+// constants at `band_base` and its component keys at `key_base`.
+void build_tables(const PagePlan& p, uint32_t block_base, uint32_t band_base, uint32_t key_base,
+                  uint32_t cap, uint32_t pcap, std::vector<BlockDesc>* blocks,
+                  std::vector<BandParam>* bands, std::vector<CompParam>* comps) {
+  blocks->resize((size_t)block_base + p.nblocks);
   for (const BandGeom& g : p.bands) {
     for (int by = 0; by < g.ncby; ++by)
       for (int bx = 0; bx < g.ncbx; ++bx) {
-        uint32_t idx = g.first_block + (uint32_t)(by * g.ncbx + bx);
+        uint32_t idx = block_base + g.first_block + (uint32_t)(by * g.ncbx + bx);
         BlockDesc& d = (*blocks)[idx];
         int x0 = g.x0 + bx * p.cbw, y0 = g.y0 + by * p.cbh;
         d.coef_slot = idx;
@@ -142,8 +187,8 @@ void build_tables(const PagePlan& p, std::vector<BlockDesc>* blocks, std::vector
         d.h = (uint16_t)(std::min(y0 + p.cbh, g.y1) - y0);
         d.orient = (uint8_t)g.orient;
         d.mb = (uint8_t)std::min(g.mb, 255);
-        d.band_param = (uint16_t)g.quant;
-        d.comp_key = (uint32_t)g.comp;
+        d.band_param = (uint16_t)(band_base + (uint32_t)g.quant);
+        d.comp_key = key_base + (uint32_t)g.comp;
         d.out_off = idx * cap;
         d.out_cap = cap;
         d.pass_off = idx * pcap;
@@ -151,7 +196,6 @@ void build_tables(const PagePlan& p, std::vector<BlockDesc>* blocks, std::vector
   }
   // PCRD band constants (rate.rs:43-85, pcrd.rs:728-748), one per quant entry.
   const int nres = p.levels + 1;
-  bands->clear();
   for (const BandQuant& q : p.quants) {
     BandParam bp{};
     int level = q.orient == LL ? std::max(nres - 1, 0) : std::max(std::max(nres - 1, 0) - q.res, 0);
@@ -167,7 +211,6 @@ void build_tables(const PagePlan& p, std::vector<BlockDesc>* blocks, std::vector
     bp.is_ll = q.orient == LL;
     bands->push_back(bp);
   }
-  comps->clear();
   for (int c = 0; c < p.ncomp; ++c) {
     CompParam cp{};
     cp.lambda_raw = p.lambda_raw;
@@ -180,8 +223,8 @@ void build_tables(const PagePlan& p, std::vector<BlockDesc>* blocks, std::vector
 }
 
 // Runs colour+DWT+quantisation for the page whose interleaved pixels are at
-// `d_px` on the device, filling code-block storage.
-int run_dwt(jp2g_ctx* c, const PagePlan& p, const uint8_t* d_px) {
+// `d_px` on the device, filling the code-block slots from `block_base` on.
+int run_dwt(jp2g_ctx* c, const PagePlan& p, const uint8_t* d_px, uint32_t block_base) {
   const int L = p.levels;
   size_t llw = (p.width + 1) / 2, llh = (p.height + 1) / 2;
   size_t ll_elems = llw * llh * p.ncomp;
@@ -192,7 +235,7 @@ int run_dwt(jp2g_ctx* c, const PagePlan& p, const uint8_t* d_px) {
     for (const BandGeom& g : p.bands) {
       if (g.res != res) continue;
       DwtBandOut& o = a.band[g.comp][g.orient];
-      o.first_block = g.first_block;
+      o.first_block = block_base + g.first_block;
       o.ncbx = std::max(g.ncbx, 1);
       o.step = p.quants[g.quant].step_f32;
     }
@@ -258,35 +301,103 @@ int run_dwt(jp2g_ctx* c, const PagePlan& p, const uint8_t* d_px) {
   return kOk;
 }
 
-int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint32_t w,
-                uint32_t h, uint32_t ncomp, int interleaved, int quality, int format,
-                std::vector<uint8_t>* out, PagePlan* plan_out, std::vector<BlockKeep>* keep_out,
-                std::vector<BlockOut>* res_out, bool stop_after_dwt) {
-  PagePlan p;
-  Failure f{};
-  if (!build_plan(w, h, (int)ncomp, quality, format, &p, &f)) return set_err(c, f.code, f.msg);
-  if (host_px == nullptr && dev_px == nullptr) return set_err(c, kInvalidInput, "pixel pointer is null");
-  if (ncomp == 3 && host_px && !interleaved) {
-    // planar input: interleave on the host (Image::from_rgb_bytes takes RGBRGB)
+// Runs f(0..n-1) on up to `threads` host threads.
+template <class F>
+void parallel_for(size_t n, int threads, F f) {
+  const size_t t = std::min<size_t>(n, (size_t)std::max(threads, 1));
+  if (t <= 1) {
+    for (size_t i = 0; i < n; ++i) f(i);
+    return;
   }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  pool.reserve(t);
+  for (size_t k = 0; k < t; ++k)
+    pool.emplace_back([&] {
+      for (size_t i; (i = next.fetch_add(1)) < n;) f(i);
+    });
+  for (auto& th : pool) th.join();
+}
+
+int host_threads(jp2g_ctx* c) {
+  if (c->opt[JP2G_OPT_HOST_THREADS] > 0) return (int)c->opt[JP2G_OPT_HOST_THREADS];
+  return std::max(1, (int)std::thread::hardware_concurrency());
+}
+
+// Debug captures of a single-page wave.
+struct WaveDebug {
+  bool stop_after_dwt = false;
+  std::vector<BlockOut>* res = nullptr;
+};
+
+// Device phase of a wave of pages: plans and validation, inputs,
+// colour+DWT+quantisation per page, then Tier-1, PCRD and compaction over
+// the wave's flat code-block list (all pages' blocks, page after page), and
+// the read-back of each page's retained blocks and bytes into its job. A page
+// that fails validation or overflows a block slot is marked and the rest
+// carry on; a CUDA failure fails the wave (return code).
+int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
   std::memset(c->counters, 0, sizeof c->counters);
-  const size_t npx = (size_t)w * h * ncomp;
+  std::vector<PageJob*> live;
+  int cbw = 0;
+  uint32_t pcap = 0;
+  for (size_t i = 0; i < njobs; ++i) {
+    PageJob* j = jobs[i];
+    Failure f{};
+    j->status = kOk;
+    if (!build_plan(j->w, j->h, (int)j->ncomp, j->quality, j->format, &j->plan, &f)) {
+      j->status = f.code;
+      j->err = f.msg;
+      continue;
+    }
+    if (!j->host_px && !j->dev_px) {
+      j->status = kInvalidInput;
+      j->err = "pixel pointer is null";
+      continue;
+    }
+    if (cbw == 0) cbw = j->plan.cbw;
+    if (j->plan.cbw != cbw) {  // waves are formed per code-block size
+      j->status = kEncodeFailed;
+      j->err = "pages of one wave must share the code-block size";
+      continue;
+    }
+    pcap = std::max(pcap, pass_cap(j->plan));
+    live.push_back(j);
+  }
+  if (live.empty()) return kOk;
+  const PagePlan& p0 = live[0]->plan;
+  const uint32_t cap = slot_cap(p0);
+  const size_t slot = (size_t)p0.cbw * p0.cbh;
   std::vector<BlockDesc> blocks;
   std::vector<BandParam> bands;
   std::vector<CompParam> comps;
-  build_tables(p, &blocks, &bands, &comps);
-  const uint32_t nb = p.nblocks;
-  const size_t slot = (size_t)p.cbw * p.cbh;
-  const uint32_t pcap = pass_cap(p);
+  uint64_t nb64 = 0;
+  size_t hpx_total = 0;
+  for (PageJob* j : live) {
+    j->block_base = (uint32_t)nb64;
+    build_tables(j->plan, j->block_base, (uint32_t)bands.size(), (uint32_t)comps.size(), cap, pcap,
+                 &blocks, &bands, &comps);
+    nb64 += j->plan.nblocks;
+    if (j->host_px) {
+      j->px_off = hpx_total;
+      hpx_total += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
+    }
+  }
+  if (nb64 * cap > 0xffffffffull)
+    return set_err(c, kUnsupportedFeature,
+                   "too many code-blocks in one device wave (" + std::to_string(nb64) + ")");
+  if (bands.size() > 0xffff)
+    return set_err(c, kUnsupportedFeature, "too many pages in one device wave");
+  const uint32_t nb = (uint32_t)nb64;
   if (!reserve(c, c->coef, std::max<size_t>(nb, 1) * slot * 4) ||
-      !reserve(c, c->payload, std::max<size_t>(nb, 1) * slot_cap(p)) ||
+      !reserve(c, c->payload, std::max<size_t>(nb, 1) * cap) ||
       !reserve(c, c->passes, std::max<size_t>(nb, 1) * pcap * sizeof(PassRec)) ||
       !reserve(c, c->res, std::max<size_t>(nb, 1) * sizeof(BlockOut)) ||
       !reserve(c, c->keep, std::max<size_t>(nb, 1) * sizeof(BlockKeep)) ||
       !reserve(c, c->blocks, std::max<size_t>(nb, 1) * sizeof(BlockDesc)) ||
       !reserve(c, c->bands, bands.size() * sizeof(BandParam)) ||
       !reserve(c, c->comps, comps.size() * sizeof(CompParam)) ||
-      !reserve(c, c->maxslope, 8 * sizeof(unsigned long long)) ||
+      !reserve(c, c->maxslope, std::max<size_t>(comps.size(), 8) * sizeof(unsigned long long)) ||
       !reserve(c, c->hullp, std::max<size_t>(nb, 1) * pcap * sizeof(uint16_t)) ||
       !reserve(c, c->hulls, std::max<size_t>(nb, 1) * pcap * sizeof(double)) ||
       !reserve(c, c->hulln, std::max<size_t>(nb, 1)) ||
@@ -294,29 +405,36 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
       !reserve(c, c->scratch, ((size_t)nb / 1024 + 2) * 4) ||
       !reserve(c, c->nplanes, std::max<size_t>(nb, 1) * 4) ||
       !reserve(c, c->planebase, (size_t)(nb + 1) * 4) ||
-      !reserve(c, c->body, std::max<size_t>(nb, 1) * slot_cap(p)))
+      !reserve(c, c->body, std::max<size_t>(nb, 1) * cap))
     return kEncodeFailed;
 
-  auto t_host0 = std::chrono::steady_clock::now();
   record(c, 0);
   // ---- inputs ----
-  const uint8_t* d_px = dev_px;
-  if (host_px) {
-    if (!reserve(c, c->px, npx) || !reserve_host(c, c->hpx, npx)) return kEncodeFailed;
+  if (hpx_total > 0) {
+    if (!reserve(c, c->px, hpx_total) || !reserve_host(c, c->hpx, hpx_total)) return kEncodeFailed;
     uint8_t* staging = reinterpret_cast<uint8_t*>(c->hpx.p);
-    if (ncomp == 3 && !interleaved) {
-      const size_t n = (size_t)w * h;
-      for (size_t i = 0; i < n; ++i) {
-        staging[3 * i + 0] = host_px[i];
-        staging[3 * i + 1] = host_px[n + i];
-        staging[3 * i + 2] = host_px[2 * n + i];
+    std::vector<PageJob*> host_jobs;
+    for (PageJob* j : live)
+      if (j->host_px) host_jobs.push_back(j);
+    // Pixels go to pinned staging (interleaving planar RGB, which
+    // Image::from_rgb_bytes takes as RGBRGB) and on to the device.
+    parallel_for(host_jobs.size(), hpx_total > (64u << 20) ? host_threads(c) : 1, [&](size_t k) {
+      const PageJob* j = host_jobs[k];
+      uint8_t* dst = staging + j->px_off;
+      const size_t n = (size_t)j->w * j->h;
+      if (j->ncomp == 3 && !j->interleaved) {
+        for (size_t i = 0; i < n; ++i) {
+          dst[3 * i + 0] = j->host_px[i];
+          dst[3 * i + 1] = j->host_px[n + i];
+          dst[3 * i + 2] = j->host_px[2 * n + i];
+        }
+      } else {
+        std::memcpy(dst, j->host_px, n * j->ncomp);
       }
-    } else {
-      std::memcpy(staging, host_px, npx);
-    }
-    if (!cuda_ok(c, cudaMemcpyAsync(c->px.p, staging, npx, cudaMemcpyHostToDevice, c->stream), "H2D"))
+    });
+    if (!cuda_ok(c, cudaMemcpyAsync(c->px.p, staging, hpx_total, cudaMemcpyHostToDevice, c->stream),
+                 "H2D"))
       return kEncodeFailed;
-    d_px = reinterpret_cast<const uint8_t*>(c->px.p);
   }
   if (!cuda_ok(c, cudaMemcpyAsync(c->blocks.p, blocks.data(), nb * sizeof(BlockDesc),
                                   cudaMemcpyHostToDevice, c->stream), "H2D blocks") ||
@@ -326,28 +444,30 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
                                   cudaMemcpyHostToDevice, c->stream), "H2D comps"))
     return kEncodeFailed;
   record(c, 1);
-  // ---- colour + DWT + quantisation ----
-  if (int rc = run_dwt(c, p, d_px)) return rc;
+  // ---- colour + DWT + quantisation, page by page ----
+  for (PageJob* j : live) {
+    const uint8_t* d_px = j->dev_px ? j->dev_px : dptr<uint8_t>(c->px) + j->px_off;
+    if (int rc = run_dwt(c, j->plan, d_px, j->block_base)) return rc;
+  }
   record(c, 2);
-  if (stop_after_dwt) {
+  if (dbg && dbg->stop_after_dwt) {
     if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "DWT")) return kEncodeFailed;
-    *plan_out = p;
     return kOk;
   }
-  // ---- Tier-1 ----
+  // ---- Tier-1 over the wave's code-blocks ----
   T1Args ta{};
   ta.blocks = dptr<BlockDesc>(c->blocks);
   ta.nblocks = nb;
   ta.coef = dptr<int32_t>(c->coef);
-  ta.cbw = p.cbw;
-  ta.cbh = p.cbh;
+  ta.cbw = p0.cbw;
+  ta.cbh = p0.cbh;
   ta.out = dptr<uint8_t>(c->payload);
   ta.passes = dptr<PassRec>(c->passes);
   ta.pass_cap = pcap;
   ta.res = dptr<BlockOut>(c->res);
   ta.nplanes = dptr<uint32_t>(c->nplanes);
   ta.plane_base = dptr<uint32_t>(c->planebase);
-  ta.sym_slot = (uint32_t)(((size_t)p.cbw * p.cbh * 5 / 2 + 15) & ~size_t(15));
+  ta.sym_slot = (uint32_t)((slot * 5 / 2 + 15) & ~size_t(15));
   launch_t1_analyze(ta, c->stream);
   launch_scan_u32(ta.nplanes, 1, nb, ta.plane_base, dptr<uint32_t>(c->scratch), c->stream);
   // the number of (block, bit-plane) items sizes the symbol buffer
@@ -368,7 +488,7 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
   record(c, kEvAnalyzeEnd);
   launch_t1_model(ta, c->num_sms, c->stream);
   record(c, kEvModelEnd);
-  launch_t1_mq(ta, c->num_sms, c->stream);
+  launch_t1_mq(ta, c->num_sms, (int)c->opt[JP2G_OPT_MQ_BLOCKS_PER_WARP], c->stream);
   c->counters[5] += 5 + (nb > 1024 ? 1 : 0);
   record(c, 3);
   // ---- PCRD ----
@@ -407,12 +527,6 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
     return kEncodeFailed;
   const BlockKeep* hk = reinterpret_cast<const BlockKeep*>(c->hkeep.p);
   const uint32_t* hoff = reinterpret_cast<const uint32_t*>(c->hoffsets.p);
-  for (uint32_t i = 0; i < nb; ++i) {
-    if (hk[i].status == 1)
-      return set_err(c, kEncodeFailed, "code-block payload exceeded its device slot");
-    if (hk[i].status >= 2)
-      return set_err(c, kEncodeFailed, "code-block bit-plane count exceeds the supported maximum");
-  }
   const uint32_t total = hoff[nb];
   if (!reserve_host(c, c->hbody, std::max<size_t>(total, 1))) return kEncodeFailed;
   if (total > 0 &&
@@ -421,20 +535,27 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
     return kEncodeFailed;
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "D2H")) return kEncodeFailed;
   record(c, 6);
-  // ---- host Tier-2 + codestream ----
-  if (!assemble_codestream(p, hk, reinterpret_cast<const uint8_t*>(c->hbody.p), hoff, out, &f))
-    return set_err(c, f.code, f.msg);
-  record(c, 7);
-  record(c, 8);
-  if (c->timing) {
-    cudaEventSynchronize(c->ev[8]);
-    for (int s = 0; s < kTotal; ++s) cudaEventElapsedTime(&c->stage_ms[s], c->ev[s], c->ev[s + 1]);
-    cudaEventElapsedTime(&c->stage_ms[kTotal], c->ev[0], c->ev[8]);
-    // tier-1 split: analysis (+item list), modelling, MQ coding
-    cudaEventElapsedTime(&c->stage_ms[kNumStages + 0], c->ev[2], c->ev[kEvAnalyzeEnd]);
-    cudaEventElapsedTime(&c->stage_ms[kNumStages + 1], c->ev[kEvAnalyzeEnd], c->ev[kEvModelEnd]);
-    cudaEventElapsedTime(&c->stage_ms[kNumStages + 2], c->ev[kEvModelEnd], c->ev[3]);
-    (void)t_host0;
+  // ---- each page's share, rebased to the page ----
+  const uint8_t* hbody = reinterpret_cast<const uint8_t*>(c->hbody.p);
+  for (PageJob* j : live) {
+    const uint32_t b0 = j->block_base, n = j->plan.nblocks;
+    for (uint32_t i = 0; i < n; ++i) {
+      if (hk[b0 + i].status == 1) {
+        j->status = kEncodeFailed;
+        j->err = "code-block payload exceeded its device slot";
+        break;
+      }
+      if (hk[b0 + i].status >= 2) {
+        j->status = kEncodeFailed;
+        j->err = "code-block bit-plane count exceeds the supported maximum";
+        break;
+      }
+    }
+    if (j->status != kOk) continue;
+    j->keep.assign(hk + b0, hk + b0 + n);
+    j->offsets.resize((size_t)n + 1);
+    for (uint32_t i = 0; i <= n; ++i) j->offsets[i] = hoff[b0 + i] - hoff[b0];
+    j->body.assign(hbody + hoff[b0], hbody + hoff[b0 + n]);
   }
   const BlockOut* hr = reinterpret_cast<const BlockOut*>(c->hres.p);
   c->counters[0] = nb;
@@ -445,10 +566,80 @@ int encode_impl(jp2g_ctx* c, const uint8_t* host_px, const uint8_t* dev_px, uint
     c->counters[6] += (uint64_t)hr[i].mbp * blocks[i].w * blocks[i].h;
   }
   c->counters[4] = total;
-  if (keep_out) keep_out->assign(hk, hk + nb);
-  if (res_out) res_out->assign(hr, hr + nb);
-  if (plan_out) *plan_out = p;
+  if (dbg && dbg->res) dbg->res->assign(hr, hr + nb);
   return kOk;
+}
+
+// Host phase of one page: Tier-2 packet headers, markers and JP2 boxes.
+void finish_page(PageJob* j) {
+  if (j->status != kOk) return;
+  Failure f{};
+  if (!assemble_codestream(j->plan, j->keep.data(), j->body.data(), j->offsets.data(), &j->out, &f)) {
+    j->status = f.code;
+    j->err = f.msg;
+  }
+  j->body.clear();
+  j->body.shrink_to_fit();
+}
+
+// Reads the stage events of the last wave into stage_ms.
+void read_stage_times(jp2g_ctx* c) {
+  if (!c->timing) return;
+  cudaEventSynchronize(c->ev[8]);
+  for (int s = 0; s < kTotal; ++s) cudaEventElapsedTime(&c->stage_ms[s], c->ev[s], c->ev[s + 1]);
+  cudaEventElapsedTime(&c->stage_ms[kTotal], c->ev[0], c->ev[8]);
+  // tier-1 split: analysis (+item list), modelling, MQ coding
+  cudaEventElapsedTime(&c->stage_ms[kNumStages + 0], c->ev[2], c->ev[kEvAnalyzeEnd]);
+  cudaEventElapsedTime(&c->stage_ms[kNumStages + 1], c->ev[kEvAnalyzeEnd], c->ev[kEvModelEnd]);
+  cudaEventElapsedTime(&c->stage_ms[kNumStages + 2], c->ev[kEvModelEnd], c->ev[3]);
+}
+
+// One page through the whole pipeline (jp2g_encode and the debug entry
+// points).
+int encode_one(jp2g_ctx* c, PageJob* j, WaveDebug* dbg) {
+  PageJob* jobs[1] = {j};
+  if (int rc = run_wave(c, jobs, 1, dbg)) return rc;
+  if (j->status != kOk) return set_err(c, j->status, j->err);
+  if (dbg && dbg->stop_after_dwt) return kOk;
+  finish_page(j);
+  record(c, 7);
+  record(c, 8);
+  read_stage_times(c);
+  if (j->status != kOk) return set_err(c, j->status, j->err);
+  return kOk;
+}
+
+// Splits jobs into waves: consecutive runs of pages with the same
+// code-block size, at most `wave_blocks` code-blocks (a larger page forms a
+// wave of its own) and at most kMaxWavePages pages (band constants are
+// indexed by 16 bits, 19 per page at most).
+constexpr size_t kMaxWavePages = 3000;
+std::vector<std::vector<PageJob*>> form_waves(jp2g_ctx* c, const std::vector<PageJob*>& jobs) {
+  const uint64_t limit = c->opt[JP2G_OPT_WAVE_BLOCKS];
+  std::vector<std::vector<PageJob*>> waves;
+  std::vector<PageJob*> cur;
+  uint64_t cur_blocks = 0;
+  int cur_cbw = 0;
+  for (PageJob* j : jobs) {
+    PagePlan p;
+    Failure f{};
+    uint64_t nb = 0;
+    int cbw = cur_cbw;
+    if (build_plan(j->w, j->h, (int)j->ncomp, j->quality, j->format, &p, &f)) {
+      nb = p.nblocks;
+      cbw = p.cbw;
+    }
+    if (!cur.empty() && (cbw != cur_cbw || cur_blocks + nb > limit || cur.size() >= kMaxWavePages)) {
+      waves.push_back(std::move(cur));
+      cur.clear();
+      cur_blocks = 0;
+    }
+    if (cur.empty()) cur_cbw = cbw;
+    cur.push_back(j);
+    cur_blocks += nb;
+  }
+  if (!cur.empty()) waves.push_back(std::move(cur));
+  return waves;
 }
 
 }  // namespace
@@ -493,6 +684,14 @@ int jp2g_create(jp2g_ctx** out, int device, uint64_t hbm_budget_bytes) {
 
 void jp2g_destroy(jp2g_ctx* c) {
   if (!c) return;
+  {
+    std::lock_guard<std::mutex> lk(c->qmu);
+    c->stop = true;
+  }
+  c->qcv.notify_all();
+  c->fcv.notify_all();
+  if (c->worker.joinable()) c->worker.join();
+  if (c->finisher.joinable()) c->finisher.join();
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   DevBuf* bufs[] = {&c->px, &c->ll0, &c->ll1, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
@@ -528,10 +727,16 @@ int jp2g_encode(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, uint32_t
   if (!out || !out_len) return set_err(c, JP2G_INVALID_INPUT, "output pointer is null");
   if (!px) return set_err(c, JP2G_INVALID_INPUT, "pixel pointer is null");
   cudaSetDevice(c->device);
-  std::vector<uint8_t> bytes;
-  int rc = encode_impl(c, px, nullptr, w, h, ncomp, interleaved, quality, format, &bytes, nullptr,
-                       nullptr, nullptr, false);
-  return finish_output(c, rc, bytes, out, out_len);
+  PageJob j;
+  j.host_px = px;
+  j.w = w;
+  j.h = h;
+  j.ncomp = ncomp;
+  j.interleaved = interleaved;
+  j.quality = quality;
+  j.format = format;
+  int rc = encode_one(c, &j, nullptr);
+  return finish_output(c, rc, j.out, out, out_len);
 }
 
 int jp2g_encode_device(jp2g_ctx* c, const uint8_t* d_px, uint32_t w, uint32_t h, uint32_t ncomp,
@@ -541,10 +746,233 @@ int jp2g_encode_device(jp2g_ctx* c, const uint8_t* d_px, uint32_t w, uint32_t h,
   if (!out || !out_len) return set_err(c, JP2G_INVALID_INPUT, "output pointer is null");
   if (!d_px) return set_err(c, JP2G_INVALID_INPUT, "pixel pointer is null");
   cudaSetDevice(c->device);
-  std::vector<uint8_t> bytes;
-  int rc = encode_impl(c, nullptr, d_px, w, h, ncomp, 1, quality, format, &bytes, nullptr, nullptr,
-                       nullptr, false);
-  return finish_output(c, rc, bytes, out, out_len);
+  PageJob j;
+  j.dev_px = d_px;
+  j.w = w;
+  j.h = h;
+  j.ncomp = ncomp;
+  j.quality = quality;
+  j.format = format;
+  int rc = encode_one(c, &j, nullptr);
+  return finish_output(c, rc, j.out, out, out_len);
+}
+
+static void job_from_request(const jp2g_request& r, PageJob* j) {
+  (r.on_device ? j->dev_px : j->host_px) = r.px;
+  j->w = r.width;
+  j->h = r.height;
+  j->ncomp = r.ncomp;
+  j->interleaved = r.on_device ? 1 : r.interleaved;
+  j->quality = r.quality;
+  j->format = r.format;
+}
+
+int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t** outs,
+                      size_t* out_lens, int* status) {
+  if (!c) return JP2G_INVALID_INPUT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (n > 0 && (!reqs || !outs || !out_lens || !status))
+    return set_err(c, JP2G_INVALID_INPUT, "null request or result array");
+  cudaSetDevice(c->device);
+  std::vector<PageJob> jobs(n);
+  std::vector<PageJob*> ptrs(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    job_from_request(reqs[i], &jobs[i]);
+    ptrs[i] = &jobs[i];
+    outs[i] = nullptr;
+    out_lens[i] = 0;
+  }
+  // Host Tier-2 of wave k runs on its own thread while wave k+1 is on the
+  // device.
+  std::thread host;
+  int rc = JP2G_OK;
+  uint64_t counters[8] = {};
+  for (auto& wave : form_waves(c, ptrs)) {
+    rc = run_wave(c, wave.data(), wave.size(), nullptr);
+    for (int k = 0; k < 8; ++k) counters[k] += c->counters[k];
+    if (rc != JP2G_OK) break;
+    if (host.joinable()) host.join();
+    const int threads = host_threads(c);
+    host = std::thread([wave, threads] {
+      parallel_for(wave.size(), threads, [&](size_t i) { finish_page(wave[i]); });
+    });
+  }
+  if (host.joinable()) host.join();
+  std::memcpy(c->counters, counters, sizeof counters);
+  if (rc != JP2G_OK) {
+    for (uint32_t i = 0; i < n; ++i) status[i] = rc;
+    return rc;
+  }
+  int first_fail = JP2G_OK;
+  for (uint32_t i = 0; i < n; ++i) {
+    status[i] = jobs[i].status;
+    if (jobs[i].status == JP2G_OK) {
+      std::vector<uint8_t>& b = jobs[i].out;
+      uint8_t* p = static_cast<uint8_t*>(std::malloc(std::max<size_t>(b.size(), 1)));
+      if (!p) {
+        status[i] = JP2G_ENCODE_FAILED;
+      } else {
+        std::memcpy(p, b.data(), b.size());
+        outs[i] = p;
+        out_lens[i] = b.size();
+      }
+    } else if (first_fail == JP2G_OK) {
+      first_fail = jobs[i].status;
+      c->err = "page " + std::to_string(i) + ": " + jobs[i].err;
+    }
+  }
+  return first_fail;
+}
+
+namespace {
+
+// Worker: forms a wave from the queue (FIFO, up to the wave limits), runs
+// its device phase and hands it to the finisher.
+void worker_loop(jp2g_ctx* c) {
+  cudaSetDevice(c->device);
+  for (;;) {
+    std::vector<std::shared_ptr<Ticket>> wave;
+    {
+      std::unique_lock<std::mutex> lk(c->qmu);
+      c->qcv.wait(lk, [&] { return c->stop || !c->pending.empty(); });
+      if (c->stop && c->pending.empty()) return;
+      uint64_t blocks = 0;
+      int cbw = 0;
+      while (!c->pending.empty() && wave.size() < kMaxWavePages) {
+        const PagePlan& p = c->pending.front()->job.plan;
+        if (!wave.empty() && (p.cbw != cbw || blocks + p.nblocks > (uint64_t)c->opt[JP2G_OPT_WAVE_BLOCKS]))
+          break;
+        cbw = p.cbw;
+        blocks += p.nblocks;
+        wave.push_back(c->pending.front());
+        c->pending.pop_front();
+      }
+    }
+    std::vector<PageJob*> jobs;
+    for (auto& t : wave) jobs.push_back(&t->job);
+    int rc;
+    std::string err;
+    {
+      std::lock_guard<std::mutex> lk(c->mu);
+      rc = run_wave(c, jobs.data(), jobs.size(), nullptr);
+      if (rc != JP2G_OK) err = c->err;
+    }
+    if (rc != JP2G_OK)
+      for (PageJob* j : jobs) {
+        j->status = rc;
+        j->err = err;
+      }
+    {
+      std::lock_guard<std::mutex> lk(c->qmu);
+      c->finishing.push_back(std::move(wave));
+    }
+    c->fcv.notify_one();
+  }
+}
+
+// Finisher: Tier-2 of each finished wave's pages on the host threads, then
+// marks their tickets done.
+void finisher_loop(jp2g_ctx* c) {
+  for (;;) {
+    std::vector<std::shared_ptr<Ticket>> wave;
+    {
+      std::unique_lock<std::mutex> lk(c->qmu);
+      c->fcv.wait(lk, [&] { return !c->finishing.empty() || (c->stop && c->pending.empty()); });
+      if (c->finishing.empty()) return;
+      wave = std::move(c->finishing.front());
+      c->finishing.pop_front();
+    }
+    parallel_for(wave.size(), host_threads(c), [&](size_t i) { finish_page(&wave[i]->job); });
+    {
+      std::lock_guard<std::mutex> lk(c->qmu);
+      for (auto& t : wave) t->done = true;
+    }
+    c->dcv.notify_all();
+  }
+}
+
+}  // namespace
+
+int jp2g_submit(jp2g_ctx* c, const jp2g_request* req, uint64_t* ticket) {
+  if (!c) return JP2G_INVALID_INPUT;
+  if (!req || !ticket) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    return set_err(c, JP2G_INVALID_INPUT, "null request or ticket pointer");
+  }
+  auto t = std::make_shared<Ticket>();
+  job_from_request(*req, &t->job);
+  Failure f{};
+  if (!build_plan(t->job.w, t->job.h, (int)t->job.ncomp, t->job.quality, t->job.format, &t->job.plan, &f) ||
+      !req->px) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    return set_err(c, req->px ? f.code : JP2G_INVALID_INPUT, req->px ? f.msg : "pixel pointer is null");
+  }
+  {
+    std::lock_guard<std::mutex> lk(c->qmu);
+    if (!c->worker.joinable()) {
+      c->worker = std::thread(worker_loop, c);
+      c->finisher = std::thread(finisher_loop, c);
+    }
+    t->id = c->next_ticket++;
+    c->tickets[t->id] = t;
+    c->pending.push_back(t);
+    *ticket = t->id;
+  }
+  c->qcv.notify_one();
+  return JP2G_OK;
+}
+
+int jp2g_poll(jp2g_ctx* c, uint64_t ticket, uint8_t** out, size_t* out_len, int timeout_ms) {
+  if (!c) return JP2G_INVALID_INPUT;
+  if (!out || !out_len) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    return set_err(c, JP2G_INVALID_INPUT, "output pointer is null");
+  }
+  std::shared_ptr<Ticket> t;
+  {
+    std::unique_lock<std::mutex> lk(c->qmu);
+    auto it = c->tickets.find(ticket);
+    if (it == c->tickets.end()) {
+      lk.unlock();
+      std::lock_guard<std::mutex> g(c->mu);
+      return set_err(c, JP2G_INVALID_INPUT, "unknown ticket " + std::to_string(ticket));
+    }
+    t = it->second;
+    auto ready = [&] { return t->done; };
+    if (timeout_ms < 0) c->dcv.wait(lk, ready);
+    else if (!c->dcv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return JP2G_PENDING;
+    c->tickets.erase(ticket);
+  }
+  std::lock_guard<std::mutex> g(c->mu);
+  if (t->job.status != JP2G_OK) return set_err(c, t->job.status, t->job.err);
+  return finish_output(c, JP2G_OK, t->job.out, out, out_len);
+}
+
+int jp2g_set_option(jp2g_ctx* c, int option, int64_t value) {
+  if (!c) return JP2G_INVALID_INPUT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  switch (option) {
+    case JP2G_OPT_WAVE_BLOCKS:
+      if (value < 1) return set_err(c, JP2G_INVALID_INPUT, "wave_blocks must be at least 1");
+      break;
+    case JP2G_OPT_MQ_BLOCKS_PER_WARP:
+      if (value < 0 || value > 32) return set_err(c, JP2G_INVALID_INPUT, "mq_blocks_per_warp must be 0..32");
+      break;
+    case JP2G_OPT_HOST_THREADS:
+      if (value < 0 || value > 1024) return set_err(c, JP2G_INVALID_INPUT, "host_threads must be 0..1024");
+      break;
+    default:
+      return set_err(c, JP2G_INVALID_INPUT, "unknown option " + std::to_string(option));
+  }
+  c->opt[option] = value;
+  return JP2G_OK;
+}
+
+int jp2g_get_option(jp2g_ctx* c, int option, int64_t* value) {
+  if (!c || !value || option < 0 || option >= JP2G_NUM_OPTS) return JP2G_INVALID_INPUT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  *value = c->opt[option];
+  return JP2G_OK;
 }
 
 void jp2g_free(uint8_t* p) { std::free(p); }
@@ -580,9 +1008,17 @@ int jp2g_debug_coefficients(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t
   if (!px || !plane) return set_err(c, JP2G_INVALID_INPUT, "null pointer");
   if (comp >= ncomp) return set_err(c, JP2G_INVALID_INPUT, "component index out of range");
   cudaSetDevice(c->device);
-  PagePlan p;
-  int rc = encode_impl(c, px, nullptr, w, h, ncomp, 1, quality, 0, nullptr, &p, nullptr, nullptr, true);
+  PageJob j;
+  j.host_px = px;
+  j.w = w;
+  j.h = h;
+  j.ncomp = ncomp;
+  j.quality = quality;
+  WaveDebug dbg;
+  dbg.stop_after_dwt = true;
+  int rc = encode_one(c, &j, &dbg);
   if (rc) return rc;
+  const PagePlan& p = j.plan;
   const size_t slot = (size_t)p.cbw * p.cbh;
   std::vector<int32_t> coef((size_t)p.nblocks * slot);
   if (!cuda_ok(c, cudaMemcpy(coef.data(), c->coef.p, coef.size() * 4, cudaMemcpyDeviceToHost), "D2H"))
@@ -605,12 +1041,19 @@ int jp2g_debug_blocks(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, ui
   std::lock_guard<std::mutex> lk(c->mu);
   if (!px || !nblocks) return set_err(c, JP2G_INVALID_INPUT, "null pointer");
   cudaSetDevice(c->device);
-  PagePlan p;
-  std::vector<BlockKeep> keep;
+  PageJob j;
+  j.host_px = px;
+  j.w = w;
+  j.h = h;
+  j.ncomp = ncomp;
+  j.quality = quality;
   std::vector<BlockOut> res;
-  std::vector<uint8_t> bytes;
-  int rc = encode_impl(c, px, nullptr, w, h, ncomp, 1, quality, 0, &bytes, &p, &keep, &res, false);
+  WaveDebug dbg;
+  dbg.res = &res;
+  int rc = encode_one(c, &j, &dbg);
   if (rc) return rc;
+  const PagePlan& p = j.plan;
+  const std::vector<BlockKeep>& keep = j.keep;
   *nblocks = p.nblocks;
   for (uint32_t i = 0; i < p.nblocks && i < cap && rows; ++i) {
     int32_t* r = rows + 8 * i;

@@ -57,7 +57,8 @@ struct T1Args {
 void launch_t1_analyze(const T1Args& a, cudaStream_t st);
 void launch_t1_items(const T1Args& a, cudaStream_t st);
 void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st);
-void launch_t1_mq(const T1Args& a, int num_sms, cudaStream_t st);
+// bpw: code-blocks per warp, 1..32, or 0 for automatic.
+void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st);
 
 // Exclusive prefix sum of n uint32 values read with a stride of `stride`
 // words: out[i] = sum of in[0..i), out[n] = total. `scratch` holds

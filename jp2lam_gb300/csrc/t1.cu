@@ -637,11 +637,11 @@ void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st) {
   t1_model_kernel<<<need < cap ? need : cap, kModelWarps * 32, 0, st>>>(a);
 }
 
-void launch_t1_mq(const T1Args& a, int num_sms, cudaStream_t st) {
+void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st) {
   if (a.nblocks == 0) return;
-  // One block per warp while that keeps at most 48 warps per SM; 32 per warp
-  // beyond that.
-  const int bpw = a.nblocks <= (uint32_t)num_sms * 48u ? 1 : 32;
+  // Automatic: one block per warp while that keeps at most 48 warps per SM,
+  // 32 per warp beyond that.
+  if (bpw <= 0 || bpw > 32) bpw = a.nblocks <= (uint32_t)num_sms * 48u ? 1 : 32;
   const uint32_t per_cta = (uint32_t)bpw * kMqWarps;
   t1_mq_kernel<<<(a.nblocks + per_cta - 1) / per_cta, kMqWarps * 32, 0, st>>>(a, bpw);
 }

@@ -1,0 +1,175 @@
+"""Batched and served encoding (jp2g_encode_batch, jp2g_submit/jp2g_poll):
+every page's codestream must be byte-identical to the single-page path and
+to the oracle, alone and in any mix, whatever the wave split, the MQ
+blocks-per-warp setting or the arrival order."""
+import random
+import threading
+
+import numpy as np
+import pytest
+
+import jp2lam_gb300 as jl
+from jp2lam_gb300 import _native
+from jp2lam_gb300._native import synth_page
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng():
+    e = jl.Engine(0)
+    yield e
+    e.close()
+
+
+def _mix(n, seed, big=False):
+    """Pages of mixed size, colour, quality and format, like the uneven batch
+    (sizes scaled down so the oracle stays quick)."""
+    rng = random.Random(seed)
+    sizes = [(64, 64), (100, 70), (257, 129), (320, 413), (1, 1), (33, 7)]
+    if big:
+        sizes += [(1275, 1650)]
+    pages = []
+    for i in range(n):
+        w, h = rng.choice(sizes)
+        c = rng.choice([1, 3])
+        q = rng.choice([50, 75, 85, 100, 20])
+        fmt = rng.choice([0, 1])
+        px = synth_page(w, h, c, 5000 + i, photo_w=w // 3, photo_h=h // 3)
+        pages.append({"px": px, "w": w, "h": h, "ncomp": c, "quality": q, "fmt": fmt})
+    return pages
+
+
+def _single(eng, p):
+    return eng.encode(p["px"], p["w"], p["h"], p["ncomp"], p["quality"], p["fmt"])
+
+
+def test_batch_matches_single_and_oracle(eng, orc):
+    pages = _mix(24, 1)
+    outs = eng.encode_batch(pages)
+    for p, o in zip(pages, outs):
+        assert isinstance(o, bytes)
+        assert o == _single(eng, p)
+        assert o == orc.encode(p["px"], p["w"], p["h"], p["ncomp"], p["quality"], p["fmt"])
+
+
+@pytest.mark.parametrize("wave_blocks", [1, 7, 100, 160000])
+def test_wave_split_does_not_change_output(eng, wave_blocks):
+    pages = _mix(12, 2)
+    ref = [_single(eng, p) for p in pages]
+    old = eng.get_option(_native.OPT_WAVE_BLOCKS)
+    try:
+        eng.set_option(_native.OPT_WAVE_BLOCKS, wave_blocks)
+        assert eng.encode_batch(pages) == ref
+    finally:
+        eng.set_option(_native.OPT_WAVE_BLOCKS, old)
+
+
+@pytest.mark.parametrize("bpw", [1, 3, 8, 32])
+def test_mq_blocks_per_warp_does_not_change_output(eng, bpw):
+    pages = _mix(8, 3, big=True)
+    eng.set_option(_native.OPT_MQ_BLOCKS_PER_WARP, 0)
+    ref = eng.encode_batch(pages)
+    try:
+        eng.set_option(_native.OPT_MQ_BLOCKS_PER_WARP, bpw)
+        assert eng.encode_batch(pages) == ref
+        assert _single(eng, pages[0]) == ref[0]
+    finally:
+        eng.set_option(_native.OPT_MQ_BLOCKS_PER_WARP, 0)
+
+
+def test_batch_failure_is_per_page(eng):
+    pages = _mix(4, 4)
+    bad = dict(pages[1])
+    bad["ncomp"] = 2
+    bad["px"] = np.zeros(bad["w"] * bad["h"] * 2, np.uint8)
+    outs = eng.encode_batch([pages[0], bad, pages[2]])
+    assert outs[0] == _single(eng, pages[0])
+    assert isinstance(outs[1], jl.InvalidInput)
+    assert outs[2] == _single(eng, pages[2])
+
+
+def test_empty_batch(eng):
+    assert eng.encode_batch([]) == []
+
+
+def test_batch_planar_and_device_inputs(eng):
+    torch = pytest.importorskip("torch")
+    w, h = 301, 203
+    px = synth_page(w, h, 3, 77, photo_w=100, photo_h=60)
+    planar = np.ascontiguousarray(px.reshape(h * w, 3).T)
+    dev = torch.from_numpy(px.copy()).cuda()
+    torch.cuda.synchronize()
+    outs = eng.encode_batch([
+        {"px": px, "w": w, "h": h, "ncomp": 3, "quality": 85, "fmt": 1},
+        {"px": planar, "w": w, "h": h, "ncomp": 3, "quality": 85, "fmt": 1, "interleaved": False},
+        {"px": dev.data_ptr(), "w": w, "h": h, "ncomp": 3, "quality": 85, "fmt": 1, "on_device": True},
+    ])
+    assert outs[0] == outs[1] == outs[2] == eng.encode(px, w, h, 3, 85, 1)
+
+
+def test_option_validation(eng):
+    with pytest.raises(jl.InvalidInput):
+        eng.set_option(_native.OPT_MQ_BLOCKS_PER_WARP, 33)
+    with pytest.raises(jl.InvalidInput):
+        eng.set_option(_native.OPT_WAVE_BLOCKS, 0)
+    with pytest.raises(jl.InvalidInput):
+        eng.set_option(99, 1)
+
+
+def test_submit_poll_matches_single(eng):
+    pages = _mix(16, 5)
+    tickets = [eng.submit(p) for p in pages]
+    results = {t: eng.poll(t) for t in reversed(tickets)}
+    for p, t in zip(pages, tickets):
+        assert results[t] == _single(eng, p)
+
+
+def test_submit_from_threads_in_any_order(eng):
+    pages = _mix(20, 6)
+    ref = [_single(eng, p) for p in pages]
+    got = [None] * len(pages)
+
+    def client(idx):
+        rng = random.Random(idx)
+        mine = list(range(idx, len(pages), 4))
+        tickets = []
+        for i in mine:
+            tickets.append((i, eng.submit(pages[i])))
+            if rng.random() < 0.5:
+                threading.Event().wait(0.001 * rng.random())
+        rng.shuffle(tickets)
+        for i, t in tickets:
+            r = None
+            while r is None:
+                r = eng.poll(t, 50)
+            got[i] = r
+
+    th = [threading.Thread(target=client, args=(k,)) for k in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert got == ref
+
+
+def test_submit_rejects_invalid_before_queueing(eng):
+    with pytest.raises(jl.InvalidInput):
+        eng.submit({"px": np.zeros(4, np.uint8), "w": 2, "h": 1, "ncomp": 2, "quality": 85, "fmt": 0})
+    with pytest.raises(jl.InvalidInput):
+        eng.poll(123456789, 0)
+
+
+def test_server_and_batch_encoder_api(eng):
+    imgs = [jl.Image.from_gray_bytes(97, 61, synth_page(97, 61, 1, s).tobytes()) for s in range(3)]
+    opts = jl.EncodeOptions(85, jl.OutputFormat.JP2)
+    ref = [jl.encode(im, opts, eng) for im in imgs]
+    assert jl.BatchEncoder(opts, eng).encode_all(imgs) == ref
+    srv = jl.Server(eng)
+    tickets = [srv.submit(im, opts) for im in imgs]
+    assert [srv.result(t) for t in tickets] == ref
+    enc = jl.BatchEncoder(opts, eng)
+    other = jl.Image.from_gray_bytes(61, 97, synth_page(61, 97, 1, 9).tobytes())
+    with pytest.raises(jl.InvalidInput):
+        enc.encode_all([imgs[0], imgs[1], other])
+    assert enc.encoded_count() == 2
