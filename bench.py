@@ -13,6 +13,19 @@ e2e   : the same through the C ABI with host buffers (jp2g_encode): the
 Each step is timed with CUDA events on the engine's stream; between steps
 the L2 is flushed by writing a 256 MiB buffer (outside the timed events).
 
+Beside the headline, the same run measures the batched and served paths
+(skipped with --no-batch / --no-serve):
+  batched : 64 sRGB 2550x3300 pages at quality 75 -> JP2 in one
+            jp2g_encode_batch call (device waves over a flat code-block list),
+            device-resident and from host buffers, against the plain path
+            (one jp2g_encode per page) on the same pages;
+  uneven  : pages of mixed size {1275x1650, 2550x3300, 3400x4400, 5100x6600},
+            50% gray / 50% sRGB, quality from {50, 75, 85, 100}, photo area
+            0-40%, batched against plain (64 pages by default, --uneven-pages);
+  served  : Poisson arrivals of a 70% uneven-page / 30% 256x256 gray q60
+            thumbnail mix through jp2g_submit/jp2g_poll under a 40 GB device
+            budget, per offered rate: pages/s, MPix/s, p50/p99/p99.9 latency.
+
 --impl reference times the CPU restatement of the reference encoder (the
 reference Rust crate cannot be built here: no Rust toolchain, and its
 rayon/wide dependencies are not vendored) on the host cores, same workload.
@@ -137,6 +150,172 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _rgb_pages(n, seed0):
+    from jp2lam_gb300._native import synth_page
+    return [{"px": synth_page(2550, 3300, 3, seed0 + i, photo_w=800, photo_h=600), "w": 2550, "h": 3300,
+             "ncomp": 3, "quality": 75, "fmt": 1} for i in range(n)]
+
+
+UNEVEN_DIMS = [(1275, 1650), (2550, 3300), (3400, 4400), (5100, 6600)]
+
+
+def _uneven_page(seed):
+    """One page of the uneven mix: dimension, colour, quality and photo area
+    fraction drawn from numpy's PCG64 seeded with `seed`; content from the
+    seeded page generator."""
+    from jp2lam_gb300._native import synth_page
+    rng = np.random.default_rng(seed)
+    w, h = UNEVEN_DIMS[int(rng.integers(0, 4))]
+    c = 1 if rng.random() < 0.5 else 3
+    q = [50, 75, 85, 100][int(rng.integers(0, 4))]
+    frac = float(rng.uniform(0.0, 0.40))
+    return {"px": synth_page(w, h, c, seed, photo_frac=frac), "w": w, "h": h, "ncomp": c, "quality": q,
+            "fmt": 1}
+
+
+def _to_device(pages, torch, dev):
+    bufs = [torch.from_numpy(p["px"]).to(dev) for p in pages]
+    dpages = [dict(p, px=b.data_ptr(), on_device=True) for p, b in zip(pages, bufs)]
+    return bufs, dpages
+
+
+def _time_calls(fn, steps, warmup, stream, torch):
+    """Per-step CUDA-event times (ms) on the engine's stream; each call ends
+    with its results on the host, so the events bracket the whole call."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return times
+
+
+def bench_batched(eng, stream, torch, dev, args):
+    """64 sRGB pages per step through jp2g_encode_batch vs one jp2g_encode per
+    page, same pages."""
+    pages = _rgb_pages(args.batch_pages, 1000)
+    mpix = sum(p["w"] * p["h"] for p in pages) / 1e6
+    bufs, dpages = _to_device(pages, torch, dev)
+    torch.cuda.synchronize()
+    sizes = []
+    dev_t = _time_calls(lambda: sizes.append(sum(len(o) for o in eng.encode_batch(dpages))),
+                        args.batch_steps, 2, stream, torch)
+    st = eng.stage_times()
+    cnt = eng.counters()
+    host_t = _time_calls(lambda: eng.encode_batch(pages), args.batch_steps, 1, stream, torch)
+    plain_pages = pages[:8]
+    plain_t = _time_calls(lambda: [eng.encode_device(p["px"], p["w"], p["h"], p["ncomp"], p["quality"],
+                                                     p["fmt"]) for p in dpages[:8]], 2, 1, stream, torch)
+    plain_host_t = _time_calls(lambda: [eng.encode(p["px"], p["w"], p["h"], p["ncomp"], p["quality"], p["fmt"])
+                                        for p in plain_pages], 2, 1, stream, torch)
+    plain_mpix = sum(p["w"] * p["h"] for p in plain_pages) / 1e6
+    del bufs
+    ms = float(np.mean(dev_t))
+    return {
+        "workload": f"{len(pages)} sRGB 2550x3300 pages (seeds 1000+i, 800x600 photo), quality 75 "
+                    "(ICT + 9/7, 6 levels) -> JP2, one jp2g_encode_batch call per step; inputs "
+                    f"{sum(p['px'].size for p in pages) / 1e9:.2f} GB > L2",
+        "steps": args.batch_steps, "ms_per_step": ms,
+        "value": mpix / (ms / 1e3), "unit": "MPix/s", "pages_per_s": len(pages) / (ms / 1e3),
+        "e2e": {"value": mpix / (np.mean(host_t) / 1e3), "unit": "MPix/s",
+                "h2d_bytes_per_step": int(sum(p["px"].size for p in pages)),
+                "d2h_bytes_per_step": int(np.mean(sizes))},
+        "plain": {"value": plain_mpix / (np.mean(plain_t) / 1e3),
+                  "e2e": plain_mpix / (np.mean(plain_host_t) / 1e3), "unit": "MPix/s",
+                  "sample": "the first 8 pages, one jp2g_encode_device / jp2g_encode each"},
+        "speedup_vs_plain": (mpix / (ms / 1e3)) / (plain_mpix / (np.mean(plain_t) / 1e3)),
+        "stages_ms": st, "gpu_launches": int(cnt[5]),
+        "counters": {"code_blocks": int(cnt[0]), "passes": int(cnt[2]), "mq_symbols": int(cnt[7]),
+                     "coefficient_bitplanes": int(cnt[6])},
+        "t1_rates": {"code_blocks_per_s": cnt[0] / (st["tier1"] / 1e3) if st["tier1"] else None,
+                     "mq_symbols_per_s": cnt[7] / (st["tier1"] / 1e3) if st["tier1"] else None},
+    }
+
+
+def bench_uneven(eng, stream, torch, dev, args):
+    pages = [_uneven_page(2000 + i) for i in range(args.uneven_pages)]
+    mpix = sum(p["w"] * p["h"] for p in pages) / 1e6
+    bufs, dpages = _to_device(pages, torch, dev)
+    torch.cuda.synchronize()
+    dev_t = _time_calls(lambda: eng.encode_batch(dpages), 2, 1, stream, torch)
+    host_t = _time_calls(lambda: eng.encode_batch(pages), 2, 1, stream, torch)
+    plain_t = _time_calls(lambda: [eng.encode_device(p["px"], p["w"], p["h"], p["ncomp"], p["quality"],
+                                                     p["fmt"]) for p in dpages], 1, 1, stream, torch)
+    del bufs
+    return {"workload": f"{len(pages)} uneven pages (seeds 2000+i; sizes, colour, quality, photo "
+                        "area drawn per page), JP2, one jp2g_encode_batch call per step",
+            "mpix": mpix, "value": mpix / (np.mean(dev_t) / 1e3), "unit": "MPix/s",
+            "e2e": mpix / (np.mean(host_t) / 1e3),
+            "plain": mpix / (np.mean(plain_t) / 1e3),
+            "speedup_vs_plain": float(np.mean(plain_t) / np.mean(dev_t)),
+            "gpu_launches": int(eng.counters()[5])}
+
+
+def bench_served(jl, local, args):
+    """Poisson arrivals through submit/poll; latency = submit -> result."""
+    import queue
+    eng = jl.Engine(local, 40 << 30)
+    rng = np.random.default_rng(42)
+    from jp2lam_gb300._native import synth_page
+    big = [_uneven_page(3000 + i) for i in range(args.serve_pool)]
+    thumbs = [{"px": synth_page(256, 256, 1, 3500 + i), "w": 256, "h": 256, "ncomp": 1, "quality": 60,
+               "fmt": 1} for i in range(8)]
+    for p in big[:2] + thumbs[:2]:  # warm the pools
+        eng.poll(eng.submit(p))
+    rows = []
+    for rate in args.serve_rates:
+        n = max(1, int(rate * args.serve_seconds))
+        gaps = rng.exponential(1.0 / rate, n)
+        picks = [(thumbs if rng.random() < 0.3 else big) for _ in range(n)]
+        reqs = [pool[int(rng.integers(0, len(pool)))] for pool in picks]
+        q = queue.Queue()
+        lat = []
+
+        def collector():
+            while True:
+                item = q.get()
+                if item is None:
+                    return
+                t_sub, tk = item
+                eng.poll(tk)
+                lat.append(time.perf_counter() - t_sub)
+
+        th = threading.Thread(target=collector)
+        th.start()
+        t0 = time.perf_counter()
+        due = t0
+        for g, r in zip(gaps, reqs):
+            due += g
+            d = due - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            q.put((time.perf_counter(), eng.submit(r)))
+        q.put(None)
+        th.join()
+        wall = time.perf_counter() - t0
+        mpix = sum(r["w"] * r["h"] for r in reqs) / 1e6
+        lat_ms = np.array(lat) * 1e3
+        rows.append({"offered_pages_per_s": rate, "requests": n, "achieved_pages_per_s": n / wall,
+                     "mpix_per_s": mpix / wall, "p50_ms": float(np.percentile(lat_ms, 50)),
+                     "p99_ms": float(np.percentile(lat_ms, 99)),
+                     "p99_9_ms": float(np.percentile(lat_ms, 99.9))})
+    eng.close()
+    sustained = [r for r in rows if r["achieved_pages_per_s"] >= 0.95 * r["offered_pages_per_s"]]
+    return {"workload": "Poisson arrivals (seed 42), 70% uneven pages drawn from a pool of "
+                        f"{args.serve_pool} (seeds 3000+i) / 30% 256x256 gray q60 thumbnails, JP2, "
+                        f"{args.serve_seconds} s per offered rate, 40 GB device budget, "
+                        "latency = submit -> result on the host",
+            "rates": rows,
+            "highest_sustained_pages_per_s": max((r["offered_pages_per_s"] for r in sustained), default=None)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -144,6 +323,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--batch-pages", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--uneven-pages", type=int, default=64)
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[50, 100, 200, 400])
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-pool", type=int, default=12)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -273,6 +460,12 @@ def main():
                                 "sample": "2 encodes of the same 2550x3300 page after 1 warm-up, "
                                           f"{threads} threads (reference threading: components, "
                                           "code-blocks, 9/7 rows in parallel)"}
+    if not args.no_batch:
+        eng.set_timing(True)
+        line["batched"] = bench_batched(eng, stream, torch, f"cuda:{local}", args)
+        line["uneven"] = bench_uneven(eng, stream, torch, f"cuda:{local}", args)
+    if not args.no_serve:
+        line["served"] = bench_served(jl, local, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     eng.close()

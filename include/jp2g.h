@@ -129,17 +129,20 @@ const char* jp2g_last_error(jp2g_ctx* ctx);
 void* jp2g_stream(jp2g_ctx* ctx);
 
 /* Stage timings of the last encode, in milliseconds, measured with CUDA
- * events on the context's stream when timing is enabled:
+ * events on the context's stream when timing is enabled (for a batch: the
+ * device stages summed over its waves, [6] the host time outside them and
+ * [7] the wall time of the call):
  * [0] h2d, [1] dwt (all levels), [2] tier-1, [3] pcrd, [4] compaction,
  * [5] d2h, [6] host tier-2 + codestream, [7] total, and the tier-1 split
  * [8] analysis, [9] context modelling, [10] MQ coding. Returns the count. */
 int jp2g_set_timing(jp2g_ctx* ctx, int enabled);
 int jp2g_stage_times(jp2g_ctx* ctx, float* ms, int n);
 
-/* Work counters of the last encode: [0] code-blocks, [1] non-empty blocks,
- * [2] coding passes, [3] payload bytes before rate control, [4] bytes
- * retained, [5] kernel launches, [6] coefficient bit-planes
- * (sum over blocks of coefficients x magnitude bit-planes). */
+/* Work counters of the last encode (or batch): [0] code-blocks,
+ * [1] non-empty blocks, [2] coding passes, [3] payload bytes before rate
+ * control, [4] bytes retained, [5] kernel launches, [6] coefficient
+ * bit-planes (sum over blocks of coefficients x magnitude bit-planes),
+ * [7] MQ symbols coded. */
 int jp2g_counters(jp2g_ctx* ctx, uint64_t* out, int n);
 
 /* Inspection entry points for parity tests. */

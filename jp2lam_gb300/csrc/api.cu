@@ -90,7 +90,7 @@ struct jp2g_ctx {
   std::mutex mu;
   // device pools
   DevBuf px, ll0, ll1, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
-      hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym;
+      hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym, stats;
   // pinned host staging
   HostBuf hpx, hkeep, hoffsets, hbody, hres, hcount;
   bool timing = false;
@@ -405,7 +405,8 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
       !reserve(c, c->scratch, ((size_t)nb / 1024 + 2) * 4) ||
       !reserve(c, c->nplanes, std::max<size_t>(nb, 1) * 4) ||
       !reserve(c, c->planebase, (size_t)(nb + 1) * 4) ||
-      !reserve(c, c->body, std::max<size_t>(nb, 1) * cap))
+      !reserve(c, c->body, std::max<size_t>(nb, 1) * cap) ||
+      !reserve(c, c->stats, 64) || !reserve_host(c, c->hcount, 64))
     return kEncodeFailed;
 
   record(c, 0);
@@ -468,11 +469,12 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
   ta.nplanes = dptr<uint32_t>(c->nplanes);
   ta.plane_base = dptr<uint32_t>(c->planebase);
   ta.sym_slot = (uint32_t)((slot * 5 / 2 + 15) & ~size_t(15));
+  ta.sym_count = dptr<unsigned long long>(c->stats);
+  if (!cuda_ok(c, cudaMemsetAsync(c->stats.p, 0, 8, c->stream), "memset")) return kEncodeFailed;
   launch_t1_analyze(ta, c->stream);
   launch_scan_u32(ta.nplanes, 1, nb, ta.plane_base, dptr<uint32_t>(c->scratch), c->stream);
   // the number of (block, bit-plane) items sizes the symbol buffer
-  if (!reserve_host(c, c->hcount, 16) ||
-      !cuda_ok(c, cudaMemcpyAsync(c->hcount.p, ta.plane_base + nb, 4, cudaMemcpyDeviceToHost, c->stream),
+  if (!cuda_ok(c, cudaMemcpyAsync(c->hcount.p, ta.plane_base + nb, 4, cudaMemcpyDeviceToHost, c->stream),
                "D2H item count") ||
       !cuda_ok(c, cudaStreamSynchronize(c->stream), "tier-1 analysis"))
     return kEncodeFailed;
@@ -523,6 +525,8 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
                                   cudaMemcpyDeviceToHost, c->stream), "D2H offsets") ||
       !cuda_ok(c, cudaMemcpyAsync(c->hres.p, c->res.p, nb * sizeof(BlockOut),
                                   cudaMemcpyDeviceToHost, c->stream), "D2H results") ||
+      !cuda_ok(c, cudaMemcpyAsync(reinterpret_cast<uint8_t*>(c->hcount.p) + 8, c->stats.p, 8,
+                                  cudaMemcpyDeviceToHost, c->stream), "D2H statistics") ||
       !cuda_ok(c, cudaStreamSynchronize(c->stream), "encode kernels"))
     return kEncodeFailed;
   const BlockKeep* hk = reinterpret_cast<const BlockKeep*>(c->hkeep.p);
@@ -566,6 +570,7 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
     c->counters[6] += (uint64_t)hr[i].mbp * blocks[i].w * blocks[i].h;
   }
   c->counters[4] = total;
+  c->counters[7] = *reinterpret_cast<const uint64_t*>(reinterpret_cast<const uint8_t*>(c->hcount.p) + 8);
   if (dbg && dbg->res) dbg->res->assign(hr, hr + nb);
   return kOk;
 }
@@ -580,6 +585,24 @@ void finish_page(PageJob* j) {
   }
   j->body.clear();
   j->body.shrink_to_fit();
+}
+
+// Adds the device stages of the wave just run (events 0..6) to stage_ms.
+void add_wave_stage_times(jp2g_ctx* c) {
+  if (!c->timing) return;
+  cudaEventSynchronize(c->ev[6]);
+  float ms = 0;
+  for (int s = 0; s < kHost; ++s) {
+    cudaEventElapsedTime(&ms, c->ev[s], c->ev[s + 1]);
+    c->stage_ms[s] += ms;
+  }
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[6]);
+  c->stage_ms[kTotal] += ms;
+  const int sub[3][2] = {{2, kEvAnalyzeEnd}, {kEvAnalyzeEnd, kEvModelEnd}, {kEvModelEnd, 3}};
+  for (int k = 0; k < 3; ++k) {
+    cudaEventElapsedTime(&ms, c->ev[sub[k][0]], c->ev[sub[k][1]]);
+    c->stage_ms[kNumStages + k] += ms;
+  }
 }
 
 // Reads the stage events of the last wave into stage_ms.
@@ -697,7 +720,7 @@ void jp2g_destroy(jp2g_ctx* c) {
   DevBuf* bufs[] = {&c->px, &c->ll0, &c->ll1, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
-                    &c->itemrec, &c->sym};
+                    &c->itemrec, &c->sym, &c->stats};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   HostBuf* hb[] = {&c->hpx, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres, &c->hcount};
@@ -787,10 +810,13 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
   std::thread host;
   int rc = JP2G_OK;
   uint64_t counters[8] = {};
+  std::memset(c->stage_ms, 0, sizeof c->stage_ms);
+  const auto t0 = std::chrono::steady_clock::now();
   for (auto& wave : form_waves(c, ptrs)) {
     rc = run_wave(c, wave.data(), wave.size(), nullptr);
     for (int k = 0; k < 8; ++k) counters[k] += c->counters[k];
     if (rc != JP2G_OK) break;
+    add_wave_stage_times(c);
     if (host.joinable()) host.join();
     const int threads = host_threads(c);
     host = std::thread([wave, threads] {
@@ -799,6 +825,13 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
   }
   if (host.joinable()) host.join();
   std::memcpy(c->counters, counters, sizeof counters);
+  if (c->timing) {
+    // batch: device stages summed over waves; host = wall time not covered
+    // by them (staging, waiting for the last wave's Tier-2); total = wall.
+    const float wall = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    c->stage_ms[kHost] = std::max(0.f, wall - c->stage_ms[kTotal]);
+    c->stage_ms[kTotal] = wall;
+  }
   if (rc != JP2G_OK) {
     for (uint32_t i = 0; i < n; ++i) status[i] = rc;
     return rc;

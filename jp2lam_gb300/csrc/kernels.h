@@ -52,6 +52,7 @@ struct T1Args {
   ItemRec* item_rec;
   uint8_t* sym;          // per item: a slot of sym_slot symbol bytes
   uint32_t sym_slot;
+  unsigned long long* sym_count;  // total MQ symbols coded (statistics)
 };
 
 void launch_t1_analyze(const T1Args& a, cudaStream_t st);

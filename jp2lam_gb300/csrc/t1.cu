@@ -555,12 +555,14 @@ __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw)
   PassRec* pr = a.passes + d.pass_off;
   const uint32_t base = a.plane_base[b];
   int pi = 0;
+  uint32_t nsym = 0;
   for (int j = 0; j < mbp; ++j) {
     // item j codes bit-plane mbp-1-j: SP | MR | CL, or CL alone for j = 0
     const ItemRec r = a.item_rec[base + j];
     const uint8_t bp = (uint8_t)r.bitplane;
     const int total = (int)(r.n_sp + r.n_mr + r.n_cl);
     const int npass = j == 0 ? 1 : 3;
+    nsym += (uint32_t)total;
     int end[3];  // symbol index at which each pass ends
     end[0] = j == 0 ? total : (int)r.n_sp;
     end[1] = (int)(r.n_sp + r.n_mr);
@@ -604,6 +606,7 @@ __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw)
   o.payload_len = (uint32_t)(m.last == 0xffu ? m.pos - 1 : m.pos);  // take_bytes
   o.status = m.ovf ? 1 : 0;
   a.res[b] = o;
+  atomicAdd(a.sym_count, (unsigned long long)nsym);
 }
 
 }  // namespace
