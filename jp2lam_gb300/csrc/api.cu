@@ -319,9 +319,12 @@ void parallel_for(size_t n, int threads, F f) {
   for (auto& th : pool) th.join();
 }
 
+// Host threads for staging and Tier-2. By default two hardware threads stay
+// free for the thread that launches the next wave and waits on the stream,
+// so overlapped Tier-2 never delays the device.
 int host_threads(jp2g_ctx* c) {
   if (c->opt[JP2G_OPT_HOST_THREADS] > 0) return (int)c->opt[JP2G_OPT_HOST_THREADS];
-  return std::max(1, (int)std::thread::hardware_concurrency());
+  return std::max(1, (int)std::thread::hardware_concurrency() - 2);
 }
 
 // Debug captures of a single-page wave.

@@ -107,18 +107,24 @@ __global__ void __launch_bounds__(NT) dwt_level_kernel(DwtLevelArgs a) {
   using C = Cfg<REV>;
   using T = typename C::T;
   constexpr int HALO = C::HALO, SW = C::SW, SH = C::SH, P = C::PITCH;
+  constexpr int TX = 32, TY = NT / 32;
   __shared__ T s[SH * P];
 
   const int comp = blockIdx.z;
   const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
   const int rw = a.rw, rh = a.rh;
-  const int tid = threadIdx.x;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
 
   // ---- load tile + halo (mirrored at the region borders) ----
-  for (int i = tid; i < SH * SW; i += NT) {
-    int ly = i / SW, lx = i - ly * SW;
-    int gy = sym(y0 - HALO + ly, rh), gx = sym(x0 - HALO + lx, rw);
-    s[ly * P + lx] = load_sample<REV>(a, comp, gx, gy);
+  const bool inner_x = x0 - HALO >= 0 && x0 - HALO + SW <= rw;
+  for (int ly = ty; ly < SH; ly += TY) {
+    int gy = y0 - HALO + ly;
+    if ((unsigned)gy >= (unsigned)rh) gy = sym(gy, rh);
+    for (int lx = tx; lx < SW; lx += TX) {
+      int gx = x0 - HALO + lx;
+      if (!inner_x && (unsigned)gx >= (unsigned)rw) gx = sym(gx, rw);
+      s[ly * P + lx] = load_sample<REV>(a, comp, gx, gy);
+    }
   }
   __syncthreads();
 
@@ -130,121 +136,255 @@ __global__ void __launch_bounds__(NT) dwt_level_kernel(DwtLevelArgs a) {
     if (rh >= 2) {
       if constexpr (REV) {
         // predict on odd rows, update on even rows (rev53.rs:419-497)
+        #pragma unroll
         for (int step = 0; step < 2; ++step) {
           const int first = step == 0 ? 1 : 2;
-          const int nrows = (SH - 2 - first) / 2 + 1;
-          for (int i = tid; i < nrows * SW; i += NT) {
-            int r = i / SW, lx = i - r * SW;
-            int ly = first + 2 * r;
-            int32_t up = s[(ly - 1) * P + lx], dn = s[(ly + 1) * P + lx];
-            if (step == 0) s[ly * P + lx] -= (up + dn) >> 1;
-            else s[ly * P + lx] += (up + dn + 2) >> 2;
-          }
+          for (int ly = first + 2 * ty; ly <= SH - 2; ly += 2 * TY)
+            for (int lx = tx; lx < SW; lx += TX) {
+              int32_t up = s[(ly - 1) * P + lx], dn = s[(ly + 1) * P + lx];
+              if (step == 0) s[ly * P + lx] -= (up + dn) >> 1;
+              else s[ly * P + lx] += (up + dn + 2) >> 2;
+            }
           __syncthreads();
         }
       } else {
         // alpha (odd), beta (even), gamma (odd), delta (even), then scale
         // (irrev97.rs:261-336)
+        #pragma unroll
         for (int step = 0; step < 4; ++step) {
           const int first = (step & 1) ? 2 : 1;
-          const int nrows = (SH - 2 - first) / 2 + 1;
           const float c = step == 0 ? kAlpha : step == 1 ? kBeta : step == 2 ? kGamma : kDelta;
-          for (int i = tid; i < nrows * SW; i += NT) {
-            int r = i / SW, lx = i - r * SW;
-            int ly = first + 2 * r;
-            s[ly * P + lx] = lift97(s[ly * P + lx], c, s[(ly - 1) * P + lx], s[(ly + 1) * P + lx]);
-          }
+          for (int ly = first + 2 * ty; ly <= SH - 2; ly += 2 * TY)
+            for (int lx = tx; lx < SW; lx += TX)
+              s[ly * P + lx] = lift97(s[ly * P + lx], c, s[(ly - 1) * P + lx], s[(ly + 1) * P + lx]);
           __syncthreads();
         }
-        for (int i = tid; i < SH * SW; i += NT) {
-          int ly = i / SW, lx = i - ly * SW;
-          s[ly * P + lx] = __fmul_rn(s[ly * P + lx], (ly & 1) ? kK : kInvK);
+        for (int ly = ty; ly < SH; ly += TY) {
+          const float k = (ly & 1) ? kK : kInvK;
+          for (int lx = tx; lx < SW; lx += TX) s[ly * P + lx] = __fmul_rn(s[ly * P + lx], k);
         }
         __syncthreads();
       }
     } else {
       if constexpr (!REV) {  // height 1: scale by 1/K (irrev97.rs:271-275)
-        for (int i = tid; i < SH * SW; i += NT) {
-          int ly = i / SW, lx = i - ly * SW;
-          s[ly * P + lx] = __fmul_rn(s[ly * P + lx], kInvK);
-        }
+        for (int ly = ty; ly < SH; ly += TY)
+          for (int lx = tx; lx < SW; lx += TX) s[ly * P + lx] = __fmul_rn(s[ly * P + lx], kInvK);
         __syncthreads();
       }
     }
     // ---- horizontal pass over the centre rows ----
     if (rw >= 2) {
       if constexpr (REV) {
+        #pragma unroll
         for (int step = 0; step < 2; ++step) {
           const int first = step == 0 ? 1 : 2;
-          const int ncols = (SW - 2 - first) / 2 + 1;
-          for (int i = tid; i < ncols * TH; i += NT) {
-            int r = i / ncols, ci = i - r * ncols;
-            int ly = HALO + r, lx = first + 2 * ci;
-            int32_t l = s[ly * P + lx - 1], rr = s[ly * P + lx + 1];
-            if (step == 0) s[ly * P + lx] -= (l + rr) >> 1;
-            else s[ly * P + lx] += (l + rr + 2) >> 2;
+          for (int r = ty; r < TH; r += TY) {
+            T* row = s + (HALO + r) * P;
+            for (int lx = first + 2 * tx; lx <= SW - 2; lx += 2 * TX) {
+              int32_t l = row[lx - 1], rr = row[lx + 1];
+              if (step == 0) row[lx] -= (l + rr) >> 1;
+              else row[lx] += (l + rr + 2) >> 2;
+            }
           }
           __syncthreads();
         }
       } else {
+        #pragma unroll
         for (int step = 0; step < 4; ++step) {
           const int first = (step & 1) ? 2 : 1;
-          const int ncols = (SW - 2 - first) / 2 + 1;
           const float c = step == 0 ? kAlpha : step == 1 ? kBeta : step == 2 ? kGamma : kDelta;
-          for (int i = tid; i < ncols * TH; i += NT) {
-            int r = i / ncols, ci = i - r * ncols;
-            int ly = HALO + r, lx = first + 2 * ci;
-            s[ly * P + lx] = lift97(s[ly * P + lx], c, s[ly * P + lx - 1], s[ly * P + lx + 1]);
+          for (int r = ty; r < TH; r += TY) {
+            T* row = s + (HALO + r) * P;
+            for (int lx = first + 2 * tx; lx <= SW - 2; lx += 2 * TX)
+              row[lx] = lift97(row[lx], c, row[lx - 1], row[lx + 1]);
           }
           __syncthreads();
         }
-        for (int i = tid; i < TH * SW; i += NT) {
-          int r = i / SW, lx = i - r * SW;
-          s[(HALO + r) * P + lx] = __fmul_rn(s[(HALO + r) * P + lx], (lx & 1) ? kK : kInvK);
-        }
-        __syncthreads();
+        // the column scale (1/K even, K odd) is applied as the samples are
+        // written out
       }
     } else {
       if constexpr (!REV) {  // width 1: scale by 1/K (irrev97.rs:95-97)
-        for (int i = tid; i < TH * SW; i += NT) {
-          int r = i / SW, lx = i - r * SW;
-          s[(HALO + r) * P + lx] = __fmul_rn(s[(HALO + r) * P + lx], kInvK);
-        }
+        for (int r = ty; r < TH; r += TY)
+          for (int lx = tx; lx < SW; lx += TX) s[(HALO + r) * P + lx] = __fmul_rn(s[(HALO + r) * P + lx], kInvK);
         __syncthreads();
       }
     }
   }
 
   // ---- write subbands ----
-  // Within a tile row, the first TW/2 threads take the even (low) columns and
-  // the rest the odd (high) ones, so each warp writes a contiguous run of one
-  // band row.
+  // Within a tile row, the first TW/2 columns of the loop take the even
+  // (low) samples and the rest the odd (high) ones, so each warp writes a
+  // contiguous run of one band row.
+  const int cbs = __ffs(a.cbw) - 1, cbhs = __ffs(a.cbh) - 1;  // code-blocks are 2^k
   const int cbw = a.cbw, cbh = a.cbh;
-  const size_t slot = (size_t)cbw * cbh;
-  for (int i = tid; i < TH * TW; i += NT) {
-    int ly = i / TW, j = i - ly * TW;
-    int lx = a.no_transform ? j : (j < TW / 2 ? 2 * j : 2 * (j - TW / 2) + 1);
-    int gy = y0 + ly, gx = x0 + lx;
-    if (gy >= rh || gx >= rw) continue;
-    T v = s[(HALO + ly) * P + HALO + lx];
-    int orient, u, vv;
-    if (a.no_transform) {
-      orient = 0; u = gx; vv = gy;
-    } else {
-      orient = ((gy & 1) << 1) | (gx & 1);  // LL, HL, LH, HH
-      u = gx >> 1; vv = gy >> 1;
+  const bool col_scale = !REV && !a.no_transform && rw >= 2;
+  for (int ly = ty; ly < TH; ly += TY) {
+    const int gy = y0 + ly;
+    if (gy >= rh) break;
+    const T* row = s + (HALO + ly) * P + HALO;
+    for (int j = tx; j < TW; j += TX) {
+      const int lx = a.no_transform ? j : (j < TW / 2 ? 2 * j : 2 * (j - TW / 2) + 1);
+      const int gx = x0 + lx;
+      if (gx >= rw) continue;
+      T v = row[lx];
+      if constexpr (!REV) {
+        if (col_scale) v = __fmul_rn(v, (lx & 1) ? kK : kInvK);
+      }
+      int orient, u, vv;
+      if (a.no_transform) {
+        orient = 0; u = gx; vv = gy;
+      } else {
+        orient = ((gy & 1) << 1) | (gx & 1);  // LL, HL, LH, HH
+        u = gx >> 1; vv = gy >> 1;
+      }
+      if (orient == 0 && a.ll != nullptr) {
+        T* ll = reinterpret_cast<T*>(a.ll);
+        ll[(size_t)comp * a.ll_comp + (size_t)vv * a.ll_pitch + u] = v;
+        continue;
+      }
+      const DwtBandOut& bo = a.band[comp][orient];
+      const uint32_t blk = bo.first_block + (uint32_t)(vv >> cbhs) * bo.ncbx + (uint32_t)(u >> cbs);
+      int32_t q;
+      if constexpr (REV) q = v;
+      else q = quantize(v, bo.step);
+      a.coef[((size_t)blk << (cbs + cbhs)) + (size_t)((vv & (cbh - 1)) << cbs) + (u & (cbw - 1))] = q;
     }
-    if (orient == 0 && a.ll != nullptr) {
-      T* ll = reinterpret_cast<T*>(a.ll);
-      ll[(size_t)comp * a.ll_comp + (size_t)vv * a.ll_pitch + u] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Register-resident tile kernel (every level with a region of at least 2x2).
+//
+// A CTA of 288 threads owns a TW x TH = 128 x 64 tile plus a 4-sample halo
+// (a 136 x 72 shared-memory tile). Lifting runs on per-thread register
+// arrays of 40 samples (32 outputs plus 4 halo samples on each side, so
+// every lifting step sees its true neighbours):
+//   vertical:   272 jobs = 136 columns x 2 row halves,
+//   horizontal: 256 jobs = 64 rows x 4 column quarters.
+// Lanes take consecutive columns (vertical) or consecutive rows
+// (horizontal); the odd shared-memory pitch keeps both conflict-free. Every
+// job reads its 40 samples before a barrier and writes its 32 outputs after
+// it, so overlapping halos read the pre-step values. The epilogue walks each
+// subband's 64 x 32 part of the tile in row order, applies the column scale
+// (9/7), quantises and stores whole code-block rows.
+constexpr int RT = 288;
+constexpr int RH = 4;             // halo
+constexpr int RN = 40;            // samples per register job (32 + 2 * RH)
+constexpr int RSW = TW + 2 * RH;  // 136
+constexpr int RSH = TH + 2 * RH;  // 72
+constexpr int RP = RSW + 1;       // shared-memory pitch
+
+template <bool REV, typename T>
+__device__ __forceinline__ void lift_regs(T (&x)[RN]) {
+  if constexpr (REV) {
+    // predict on odd samples, update on even ones (rev53.rs:419-497)
+    #pragma unroll
+    for (int i = 1; i < RN - 1; i += 2) x[i] -= (x[i - 1] + x[i + 1]) >> 1;
+    #pragma unroll
+    for (int i = 2; i < RN - 1; i += 2) x[i] += (x[i - 1] + x[i + 1] + 2) >> 2;
+  } else {
+    // alpha (odd), beta (even), gamma (odd), delta (even) (irrev97.rs:261-336)
+    #pragma unroll
+    for (int i = 1; i < RN - 1; i += 2) x[i] = lift97(x[i], kAlpha, x[i - 1], x[i + 1]);
+    #pragma unroll
+    for (int i = 2; i < RN - 2; i += 2) x[i] = lift97(x[i], kBeta, x[i - 1], x[i + 1]);
+    #pragma unroll
+    for (int i = 3; i < RN - 2; i += 2) x[i] = lift97(x[i], kGamma, x[i - 1], x[i + 1]);
+    #pragma unroll
+    for (int i = 4; i < RN - 4; i += 2) x[i] = lift97(x[i], kDelta, x[i - 1], x[i + 1]);
+  }
+}
+
+template <bool REV>
+__global__ void __launch_bounds__(RT) dwt_tile_kernel(DwtLevelArgs a) {
+  using T = typename Cfg<REV>::T;
+  __shared__ T s[RSH * RP];
+  const int comp = blockIdx.z;
+  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+  const int rw = a.rw, rh = a.rh;
+  const int tid = threadIdx.x;
+
+  // ---- load tile + halo (mirrored at the region borders) ----
+  {
+    const int tx = tid & 31, ty = tid >> 5, nty = RT / 32;
+    const bool inner_x = x0 - RH >= 0 && x0 - RH + RSW <= rw;
+    for (int ly = ty; ly < RSH; ly += nty) {
+      int gy = y0 - RH + ly;
+      if ((unsigned)gy >= (unsigned)rh) gy = sym(gy, rh);
+      for (int lx = tx; lx < RSW; lx += 32) {
+        int gx = x0 - RH + lx;
+        if (!inner_x && (unsigned)gx >= (unsigned)rw) gx = sym(gx, rw);
+        s[ly * RP + lx] = load_sample<REV>(a, comp, gx, gy);
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- vertical lifting: column lx, rows [32 h, 32 h + 40) ----
+  {
+    T x[RN];
+    const int job = tid;  // 272 jobs, 288 threads
+    const bool active = job < 2 * RSW;
+    const int h = job >= RSW ? 1 : 0, lx = job - h * RSW, r0 = 32 * h;
+    if (active) {
+      #pragma unroll
+      for (int i = 0; i < RN; ++i) x[i] = s[(r0 + i) * RP + lx];
+    }
+    __syncthreads();
+    if (active) {
+      lift_regs<REV>(x);
+      #pragma unroll
+      for (int i = RH; i < RN - RH; ++i) {
+        T v = x[i];
+        if constexpr (!REV) v = __fmul_rn(v, (i & 1) ? kK : kInvK);  // rows: 1/K even, K odd
+        s[(r0 + i) * RP + lx] = v;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- horizontal lifting: row RH + r, columns [32 q, 32 q + 40) ----
+  {
+    T x[RN];
+    const int job = tid;  // 256 jobs
+    const bool active = job < 4 * TH;
+    const int q = job / TH, r = job - q * TH, c0 = 32 * q;
+    T* row = s + (RH + r) * RP;
+    if (active) {
+      #pragma unroll
+      for (int i = 0; i < RN; ++i) x[i] = row[c0 + i];
+    }
+    __syncthreads();
+    if (active) {
+      lift_regs<REV>(x);
+      #pragma unroll
+      for (int i = RH; i < RN - RH; ++i) row[c0 + i] = x[i];
+    }
+  }
+  __syncthreads();
+
+  // ---- epilogue: subbands in row order, quantised into code-block slots ----
+  const int cbs = __ffs(a.cbw) - 1, cbhs = __ffs(a.cbh) - 1;
+  const int u0 = x0 >> 1, v0 = y0 >> 1;
+  const int bw_lo = (rw + 1) >> 1, bw_hi = rw >> 1, bh_lo = (rh + 1) >> 1, bh_hi = rh >> 1;
+  for (int idx = tid; idx < 4 * 32 * 64; idx += RT) {
+    const int band = idx >> 11, rr = (idx >> 6) & 31, cc = idx & 63;  // band: LL, HL, LH, HH
+    const int u = u0 + cc, v = v0 + rr;
+    const int bw = (band & 1) ? bw_hi : bw_lo, bh = (band & 2) ? bh_hi : bh_lo;
+    if (u >= bw || v >= bh) continue;
+    T val = s[(RH + 2 * rr + (band >> 1)) * RP + RH + 2 * cc + (band & 1)];
+    if constexpr (!REV) val = __fmul_rn(val, (band & 1) ? kK : kInvK);  // columns: 1/K even, K odd
+    if (band == 0 && a.ll != nullptr) {
+      reinterpret_cast<T*>(a.ll)[(size_t)comp * a.ll_comp + (size_t)v * a.ll_pitch + u] = val;
       continue;
     }
-    const DwtBandOut& bo = a.band[comp][orient];
-    uint32_t blk = bo.first_block + (uint32_t)(vv / cbh) * bo.ncbx + (uint32_t)(u / cbw);
-    int32_t q;
-    if constexpr (REV) q = v;
-    else q = quantize(v, bo.step);
-    a.coef[(size_t)blk * slot + (size_t)(vv % cbh) * cbw + (u % cbw)] = q;
+    const DwtBandOut& bo = a.band[comp][band];
+    const uint32_t blk = bo.first_block + (uint32_t)(v >> cbhs) * bo.ncbx + (uint32_t)(u >> cbs);
+    int32_t qv;
+    if constexpr (REV) qv = val;
+    else qv = quantize(val, bo.step);
+    a.coef[((size_t)blk << (cbs + cbhs)) + ((size_t)(v & (a.cbh - 1)) << cbs) + (u & (a.cbw - 1))] = qv;
   }
 }
 
@@ -252,6 +392,12 @@ __global__ void __launch_bounds__(NT) dwt_level_kernel(DwtLevelArgs a) {
 
 void launch_dwt_level(const DwtLevelArgs& a, bool reversible, cudaStream_t st) {
   dim3 grid((a.rw + TW - 1) / TW, (a.rh + TH - 1) / TH, a.ncomp);
+  if (!a.no_transform && a.rw >= 2 && a.rh >= 2) {
+    if (reversible) dwt_tile_kernel<true><<<grid, RT, 0, st>>>(a);
+    else dwt_tile_kernel<false><<<grid, RT, 0, st>>>(a);
+    return;
+  }
+  // zero levels, or a one-sample-wide/high region (its own scaling rules)
   if (reversible) dwt_level_kernel<true><<<grid, NT, 0, st>>>(a);
   else dwt_level_kernel<false><<<grid, NT, 0, st>>>(a);
 }

@@ -448,23 +448,28 @@ __device__ __forceinline__ void mq_byteout(Mq& m) {
   else m.ovf = 1;
 }
 
-// One MQ symbol (C.2.4-C.2.7). `e` is the context's state entry; returns the
-// entry the context holds afterwards. The exchange is predicated; the only
-// branch is the rare one that emits bytes.
-__device__ __forceinline__ uint32_t mq_step(Mq& m, uint32_t e, uint32_t bit, const uint32_t* T) {
-  const uint32_t qe = e & 0xffffu;
-  const bool is_mps = bit == ((e >> 16) & 1u);
+// Probability-state entry of a context, in shared memory: x = qe |
+// (leading zeros of qe in 16 bits) << 16 | MPS << 20; y = index of the next
+// state after an MPS renormalisation | index after an LPS << 8 (indices
+// into the 94-entry table of (state, MPS) pairs).
+//
+// One MQ symbol (C.2.4-C.2.7) with the decisions folded: after A -= qe the
+// coder keeps A (and adds qe to C) exactly when (A < qe) equals "LPS", and
+// otherwise takes qe (C unchanged). A stays >= 0x8000 between symbols and qe
+// <= 0x5601, so a kept A is either >= 0x8000 (no renormalisation) or in
+// [0x29ff, 0x8000) (a shift of 1 or 2), while a taken qe shifts by its
+// stored leading-zero count. The context moves to its next state exactly
+// when the shift is non-zero. Returns the context's new entry.
+__device__ __forceinline__ uint2 mq_step(Mq& m, uint2 e, uint32_t sym, const uint2* T) {
+  const uint32_t qe = e.x & 0xffffu;
+  const uint32_t lps = ((e.x >> 20) ^ sym) & 1u;
   const uint32_t a = m.a - qe;
-  const bool ren = !is_mps || (a & 0x8000u) == 0;
-  const bool lt = a < qe;
-  const bool add_c = is_mps ? (!ren || !lt) : lt;
-  const bool take_qe = is_mps ? (ren && lt) : !lt;
-  m.c += add_c ? qe : 0u;
-  const uint32_t na = take_qe ? qe : a;
-  uint32_t ne = e;
-  if (ren) ne = T[is_mps ? ((e >> 17) & 0x7fu) : (e >> 24)];
-  uint32_t n = __clz(na) - 16;  // RENORME in one step
-  m.a = na << n;
+  const bool take_a = (a < qe) == (lps != 0);
+  uint32_t n = take_a ? (a < 0x4000u ? 2u : (a < 0x8000u ? 1u : 0u)) : ((e.x >> 16) & 15u);
+  m.c += take_a ? qe : 0u;
+  m.a = (take_a ? a : qe) << n;
+  uint2 ne = e;
+  if (n) ne = T[lps ? (e.y >> 8) : (e.y & 0xffu)];
   if (n >= m.ct) {
     do {
       m.c <<= m.ct;
@@ -495,15 +500,15 @@ __device__ __forceinline__ uint32_t chunk_sym(const uint4& q, int i) {
 
 // Codes all 16 symbols of a chunk, the next symbol's context entry loaded
 // one step ahead of its use.
-__device__ __forceinline__ void mq_chunk16(Mq& m, uint32_t* ce, const uint32_t* T, const uint4 q) {
+__device__ __forceinline__ void mq_chunk16(Mq& m, uint2* ce, const uint2* T, const uint4 q) {
   uint32_t sym = q.x & 0xffu;
-  uint32_t e = ce[32 * (sym >> 1)];
+  uint2 e = ce[32 * (sym >> 1)];
   #pragma unroll
   for (int i = 0; i < 16; ++i) {
     const uint32_t symn = i < 15 ? chunk_sym(q, i + 1) : 0u;
     const uint32_t cx = sym >> 1, cxn = symn >> 1;
-    uint32_t en = i < 15 ? ce[32 * cxn] : 0u;
-    const uint32_t ne = mq_step(m, e, sym & 1u, T);
+    uint2 en = i < 15 ? ce[32 * cxn] : make_uint2(0u, 0u);
+    const uint2 ne = mq_step(m, e, sym, T);
     ce[32 * cx] = ne;
     if (cxn == cx) en = ne;
     e = en;
@@ -513,12 +518,12 @@ __device__ __forceinline__ void mq_chunk16(Mq& m, uint32_t* ce, const uint32_t* 
 
 // Codes symbols [from, to) of a chunk one at a time (chunks that hold a pass
 // end or the end of the stream).
-__device__ __forceinline__ void mq_chunk_part(Mq& m, uint32_t* ce, const uint32_t* T, const uint4 q,
+__device__ __forceinline__ void mq_chunk_part(Mq& m, uint2* ce, const uint2* T, const uint4 q,
                                               int from, int to) {
   for (int i = from; i < to; ++i) {
     const uint32_t sym = chunk_sym(q, i);
     const uint32_t cx = sym >> 1;
-    ce[32 * cx] = mq_step(m, ce[32 * cx], sym & 1u, T);
+    ce[32 * cx] = mq_step(m, ce[32 * cx], sym, T);
   }
 }
 
@@ -528,18 +533,20 @@ __device__ __forceinline__ void mq_chunk_part(Mq& m, uint32_t* ce, const uint32_
 // longest block's serial chain sets the time (lanes of a warp diverge on
 // every byte emitted, which lengthens each lane's chain).
 __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw) {
-  __shared__ uint32_t T[94];
-  __shared__ uint32_t ce_all[kMqWarps][20 * 32];
+  __shared__ uint2 T[94];
+  __shared__ uint2 ce_all[kMqWarps][20 * 32];
   for (int i = threadIdx.x; i < 94; i += blockDim.x) {
-    // expand (qe | nmps << 16 | nlps << 24) to (qe | mps << 16 | nmps << 17 | nlps << 24)
+    // (qe | nmps << 16 | nlps << 24) -> the entry layout of mq_step
     const uint32_t v = c_tables.mq[i];
-    T[i] = (v & 0xffffu) | ((uint32_t)(i & 1) << 16) | (((v >> 16) & 0x7fu) << 17) | ((v >> 24) << 24);
+    const uint32_t qe = v & 0xffffu;
+    T[i] = make_uint2(qe | ((uint32_t)(__clz(qe) - 16) << 16) | ((uint32_t)(i & 1) << 20),
+                      ((v >> 16) & 0xffu) | (((v >> 24) & 0xffu) << 8));
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   if (lane >= bpw) return;
-  uint32_t* ce = &ce_all[wid][lane];  // context c at ce[32 * c]
+  uint2* ce = &ce_all[wid][lane];  // context c at ce[32 * c]
   const uint32_t b = (blockIdx.x * kMqWarps + wid) * (uint32_t)bpw + (uint32_t)lane;
   if (b >= a.nblocks) return;
   BlockOut o = a.res[b];
