@@ -49,7 +49,6 @@ struct Tables {
 // Built on the host from the standard's rules, copied in by upload_t1_tables.
 __constant__ Tables c_tables;
 
-__device__ __forceinline__ uint32_t bitat(uint64_t m, int x) { return (uint32_t)(m >> x) & 1u; }
 __device__ __forceinline__ uint64_t westm(uint64_t m) { return m << 1; }   // bit x = m[x-1]
 __device__ __forceinline__ uint64_t eastm(uint64_t m) { return m >> 1; }   // bit x = m[x+1]
 __device__ __forceinline__ uint64_t dil(uint64_t m) { return m | (m << 1) | (m >> 1); }
@@ -106,34 +105,25 @@ struct ModelSmem {
   uint64_t V[64];   // visited (coded) in SP
 };
 
-struct Emitter {
-  uint64_t lo = 0, hi = 0;
-  int n = 0;
-  __device__ __forceinline__ void push(uint32_t s) {
-    hi = (hi << 8) | (lo >> 56);
-    lo = (lo << 8) | s;
-    ++n;
-  }
-  __device__ __forceinline__ uint32_t at(int i) const {  // i-th pushed symbol
-    int b = n - 1 - i;
-    return b < 8 ? (uint32_t)(lo >> (8 * b)) & 0xffu : (uint32_t)(hi >> (8 * (b - 8))) & 0xffu;
-  }
-};
+// Each lane codes two adjacent columns, xa = 2 lane and xb = 2 lane + 1. A
+// row mask is seen through the lane's 4-bit window of columns
+// (xa-1, xa, xb, xb+1): bit 0 is the west neighbour of xa, bits 1-2 the
+// lane's own columns, bit 3 the east neighbour of xb (0 outside the block).
+__device__ __forceinline__ uint32_t win4(uint64_t m, int sh) {  // sh = 2 lane - 1
+  return (uint32_t)(sh < 0 ? (m << 1) : (m >> sh)) & 0xfu;
+}
 
-// Writes the lanes' symbols in lane (= column) order after `*pos`, returning
-// the symbols written.
-__device__ __forceinline__ uint32_t flush_symbols(const Emitter& e, uint8_t* out, uint32_t* pos,
-                                                  int lane) {
-  uint32_t incl = (uint32_t)e.n;
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-  uint8_t* dst = out + *pos + (incl - (uint32_t)e.n);
-  for (int i = 0; i < e.n; ++i) dst[i] = (uint8_t)e.at(i);
-  *pos += total;
-  return total;
+// Zero-coding neighbourhood index (bit 0 NW, 1 N, 2 NE, 3 W, 5 E, 6 SW, 7 S,
+// 8 SE) of column c (0: xa, 1: xb) from windows of the row above, the row and
+// the row below. `f` windows hold the state of samples already visited in
+// this pass (west columns, and the rows above in the same column), `p`
+// windows the state before the pass (east columns, rows below).
+__device__ __forceinline__ uint32_t zc_index(uint32_t up_f, uint32_t up_p, uint32_t f, uint32_t pr,
+                                             uint32_t dn_f, uint32_t dn_p, int c) {
+  const uint32_t up = ((up_f >> c) & 3u) | ((up_p >> c) & 4u);
+  const uint32_t mid = (((f >> c) & 1u) << 3) | (((pr >> c) & 4u) << 3);
+  const uint32_t dn = (((dn_f >> c) & 1u) | ((dn_p >> c) & 6u)) << 6;
+  return up | mid | dn;
 }
 
 // Sign-context index from the four cardinal neighbours' significance and
@@ -150,26 +140,28 @@ struct ModelTables {
   const uint8_t* spb;
 };
 
-// Emits a zero-coding symbol for sample (x, row) and, if it becomes
-// significant, its sign symbol. `w`, `nb` etc. are the neighbour masks as
-// seen at the sample's visit.
-__device__ __forceinline__ void emit_zc(Emitter& e, const ModelTables& t, int x, uint32_t bit,
-                                        uint64_t nwm, uint64_t nm, uint64_t nem, uint64_t wm,
-                                        uint64_t em, uint64_t swm, uint64_t sm, uint64_t sem,
-                                        uint64_t sgn_w_row, uint64_t sgn_n_row, uint64_t sgn_s_row,
-                                        uint64_t sgn_row) {
-  uint32_t m8 = bitat(nwm, x) | (bitat(nm, x) << 1) | (bitat(nem, x) << 2) | (bitat(wm, x) << 3) |
-                (bitat(em, x) << 5) | (bitat(swm, x) << 6) | (bitat(sm, x) << 7) | (bitat(sem, x) << 8);
-  e.push(((uint32_t)t.zc[m8] << 1) | bit);
-  if (bit) {
-    uint32_t sw = bitat(wm, x), sn = bitat(nm, x), se = bitat(em, x), ss = bitat(sm, x);
-    uint32_t gw = x > 0 ? bitat(sgn_w_row, x - 1) : 0u;
-    uint32_t gn = bitat(sgn_n_row, x);
-    uint32_t ge = x < 63 ? bitat(sgn_w_row, x + 1) : 0u;
-    uint32_t gs = bitat(sgn_s_row, x);
-    uint32_t lu = sign_index(sw, gw, sn, gn, se, ge, ss, gs);
-    e.push(((uint32_t)t.sc[lu] << 1) | (bitat(sgn_row, x) ^ t.spb[lu]));
+// Sign symbol of column c of a row: m8 is the sample's zero-coding index
+// (its N, W, E, S bits are the significance the sign context sees); g, gu,
+// gd are the sign windows of the row, the row above and the row below.
+__device__ __forceinline__ uint32_t sign_symbol(const ModelTables& t, uint32_t m8, uint32_t g,
+                                                uint32_t gu, uint32_t gd, int c) {
+  const uint32_t sw = (m8 >> 3) & 1u, sn = (m8 >> 1) & 1u, se = (m8 >> 5) & 1u, ss = (m8 >> 7) & 1u;
+  const uint32_t gw = (g >> c) & 1u, ge = (g >> (c + 2)) & 1u;
+  const uint32_t gn = (gu >> (c + 1)) & 1u, gs = (gd >> (c + 1)) & 1u;
+  const uint32_t lu = sign_index(sw, gw, sn, gn, se, ge, ss, gs);
+  return ((uint32_t)t.sc[lu] << 1) | (((g >> (c + 1)) & 1u) ^ t.spb[lu]);
+}
+
+// Exclusive prefix of v over the warp's lanes; *total = the warp's sum.
+__device__ __forceinline__ uint32_t warp_offset(uint32_t v, int lane, uint32_t* total) {
+  uint32_t x = v;
+  #pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += t;
   }
+  *total = __shfl_sync(0xffffffffu, x, 31);
+  return x - v;
 }
 
 __global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
@@ -200,6 +192,7 @@ __global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
     const uint64_t valid = w == 64 ? ~0ull : ((1ull << w) - 1);
     const int32_t* blk = a.coef + (size_t)d.coef_slot * a.cbw * a.cbh;
     ModelTables t{s_zc + d.orient * 512, s_sc, s_spb};
+    const int sh = 2 * lane - 1;  // window of columns 2 lane - 1 .. 2 lane + 2
 
     // ---- masks for this bit-plane ----
     for (int y = 0; y < h; ++y) {
@@ -264,28 +257,38 @@ __global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
           if (k + 3 < 64) s.V[k + 3] = V3;
         }
         ns_sp += __popcll(N0) + __popcll(N1) + __popcll(N2) + __popcll(N3);
-        // emission in scan order: columns are lanes, rows top to bottom
+        // emission in scan order: within the stripe column by column (each
+        // lane: its column xa, then xb), rows top to bottom
         const uint64_t F0 = S0 | N0, F1 = S1 | N1, F2 = S2 | N2, F3 = S3 | N3;
-        const uint64_t G0 = s.Sn[k + 1], G1 = s.Sn[k + 2], G2 = s.Sn[k + 3], G3 = s.Sn[k + 4],
-                       Gp = s.Sn[k], GD = s.Sn[k + 5];
-        for (int round = 0; round * 32 < w; ++round) {
-          const int x = lane + 32 * round;
-          Emitter e;
-          if (x < w) {
-            if (bitat(V0, x))
-              emit_zc(e, t, x, bitat(B0, x), westm(Fp), Fp, eastm(Fp), westm(F0), eastm(S0), westm(F1), S1,
-                      eastm(S1), G0, Gp, G1, G0);
-            if (bitat(V1, x))
-              emit_zc(e, t, x, bitat(B1, x), westm(F0), F0, eastm(S0), westm(F1), eastm(S1), westm(F2), S2,
-                      eastm(S2), G1, G0, G2, G1);
-            if (bitat(V2, x))
-              emit_zc(e, t, x, bitat(B2, x), westm(F1), F1, eastm(S1), westm(F2), eastm(S2), westm(F3), S3,
-                      eastm(S3), G2, G1, G3, G2);
-            if (bitat(V3, x))
-              emit_zc(e, t, x, bitat(B3, x), westm(F2), F2, eastm(S2), westm(F3), eastm(S3), westm(D), D,
-                      eastm(D), G3, G2, GD, G3);
+        {
+          const uint32_t wfp = win4(Fp, sh), wd = win4(D, sh);
+          const uint32_t wf[4] = {win4(F0, sh), win4(F1, sh), win4(F2, sh), win4(F3, sh)};
+          const uint32_t wp[4] = {win4(S0, sh), win4(S1, sh), win4(S2, sh), win4(S3, sh)};
+          const uint32_t wv[4] = {win4(V0, sh), win4(V1, sh), win4(V2, sh), win4(V3, sh)};
+          const uint32_t wb[4] = {win4(B0, sh), win4(B1, sh), win4(B2, sh), win4(B3, sh)};
+          uint32_t wg[6];
+          #pragma unroll
+          for (int r = 0; r < 6; ++r) wg[r] = win4(s.Sn[k + r], sh);  // rows k-1 .. k+4
+          uint32_t cnt = 0;
+          #pragma unroll
+          for (int r = 0; r < 4; ++r) cnt += __popc(wv[r] & 6u) + __popc(wv[r] & wb[r] & 6u);
+          uint32_t total;
+          uint8_t* o = out + pos + warp_offset(cnt, lane, &total);
+          pos += total;
+          n_sp += total;
+          #pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            #pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              if (!((wv[r] >> (c + 1)) & 1u)) continue;
+              const uint32_t uf = r == 0 ? wfp : wf[r > 0 ? r - 1 : 0], up = r == 0 ? wfp : wp[r > 0 ? r - 1 : 0];
+              const uint32_t df = r == 3 ? wd : wf[r < 3 ? r + 1 : 3], dp = r == 3 ? wd : wp[r < 3 ? r + 1 : 3];
+              const uint32_t m8 = zc_index(uf, up, wf[r], wp[r], df, dp, c);
+              const uint32_t bit = (wb[r] >> (c + 1)) & 1u;
+              *o++ = (uint8_t)(((uint32_t)t.zc[m8] << 1) | bit);
+              if (bit) *o++ = (uint8_t)sign_symbol(t, m8, wg[r + 1], wg[r], wg[r + 2], c);
+            }
           }
-          n_sp += flush_symbols(e, out, &pos, lane);
         }
         Fp = F3;
         if (k + 4 > h) break;
@@ -293,22 +296,32 @@ __global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
       __syncwarp();
       // ---- magnitude refinement ----
       for (int k = 0; k < h; k += 4) {
-        const int lim = min(4, h - k);
-        for (int round = 0; round * 32 < w; ++round) {
-          const int x = lane + 32 * round;
-          Emitter e;
-          if (x < w) {
-            for (int r = 0; r < lim; ++r) {
-              const int y = k + r;
-              const uint64_t Sy = s.S[y + 1];
-              if (!bitat(Sy, x)) continue;
-              const uint64_t Gu = s.S[y] | s.N[y], Gm = Sy | s.N[y + 1], Gd = s.S[y + 2] | s.N[y + 2];
-              uint32_t nb = bitat(dil(Gu) | westm(Gm) | eastm(Gm) | dil(Gd), x);
-              uint32_t cx = bitat(s.R[y], x) ? 16u : (nb ? 15u : 14u);  // helpers.rs:36-50
-              e.push((cx << 1) | bitat(s.B[y], x));
-            }
+        uint32_t wf[6];  // state after SP of rows k-1 .. k+4
+        #pragma unroll
+        for (int r = 0; r < 6; ++r) wf[r] = win4(s.S[k + r] | s.N[k + r], sh);
+        uint32_t ws[4], wr[4], wb[4];
+        #pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          ws[r] = win4(s.S[k + r + 1], sh);
+          wr[r] = win4(s.R[k + r], sh);
+          wb[r] = win4(s.B[k + r], sh);
+        }
+        uint32_t cnt = 0;
+        #pragma unroll
+        for (int r = 0; r < 4; ++r) cnt += __popc(ws[r] & 6u);
+        uint32_t total;
+        uint8_t* o = out + pos + warp_offset(cnt, lane, &total);
+        pos += total;
+        n_mr += total;
+        #pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          #pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            if (!((ws[r] >> (c + 1)) & 1u)) continue;
+            const uint32_t nb = ((wf[r] >> c) & 7u) | ((wf[r + 1] >> c) & 5u) | ((wf[r + 2] >> c) & 7u);
+            const uint32_t cx = ((wr[r] >> (c + 1)) & 1u) ? 16u : (nb ? 15u : 14u);  // helpers.rs:36-50
+            *o++ = (uint8_t)((cx << 1) | ((wb[r] >> (c + 1)) & 1u));
           }
-          n_mr += flush_symbols(e, out, &pos, lane);
         }
       }
     } else {
@@ -347,48 +360,76 @@ __global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
                          eastm(Gr[0] | Gr[1] | Gr[2] | Gr[3]) | dil(Gd);
           clean = ~(busy | nbr) & valid;
         }
-        for (int round = 0; round * 32 < w; ++round) {
-          const int x = lane + 32 * round;
-          Emitter e;
-          if (x < w) {
+        {
+          const uint32_t wgp = win4(Gp, sh), wgd = win4(Gd, sh), wcl = win4(clean, sh);
+          uint32_t wG[4], wF[4], wC[4], wB[4], wsg[6];
+          #pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            wG[r] = win4(Gr[r], sh);
+            wF[r] = win4(Fr[r], sh);
+            wC[r] = win4(Cr[r], sh);
+            wB[r] = win4(Br[r], sh);
+          }
+          wsg[0] = win4(SgP, sh);
+          #pragma unroll
+          for (int r = 0; r < 4; ++r) wsg[r + 1] = win4(Sg[r], sh);
+          wsg[5] = win4(SgD, sh);
+          // per column: candidate rows, their bits, run-mode eligibility
+          uint32_t cm[2], bm[2], cnt = 0;
+          #pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            cm[c] = 0;
+            bm[c] = 0;
+            #pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              cm[c] |= ((wC[r] >> (c + 1)) & 1u) << r;
+              bm[c] |= ((wB[r] >> (c + 1)) & 1u) << r;
+            }
+            if ((wcl >> (c + 1)) & 1u) {
+              if (bm[c] == 0) {
+                cnt += 1;
+              } else {
+                const uint32_t after = 0xfu & ~((2u << (__ffs(bm[c]) - 1)) - 1u);
+                cnt += 4 + __popc(after) + __popc(bm[c] & after);
+              }
+            } else {
+              cnt += __popc(cm[c]) + __popc(cm[c] & bm[c]);
+            }
+          }
+          uint32_t total;
+          uint8_t* o = out + pos + warp_offset(cnt, lane, &total);
+          pos += total;
+          #pragma unroll
+          for (int c = 0; c < 2; ++c) {
             int first = 0;
-            if (bitat(clean, x)) {
-              uint32_t nib = bitat(Br[0], x) | (bitat(Br[1], x) << 1) | (bitat(Br[2], x) << 2) |
-                             (bitat(Br[3], x) << 3);
-              if (nib == 0) {
-                e.push((uint32_t)kCtxAGG << 1);
+            if ((wcl >> (c + 1)) & 1u) {
+              if (bm[c] == 0) {
+                *o++ = (uint8_t)((uint32_t)kCtxAGG << 1);
                 first = 4;
               } else {
-                const int rl = __ffs(nib) - 1;
-                e.push(((uint32_t)kCtxAGG << 1) | 1u);
-                e.push(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl >> 1));
-                e.push(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl & 1u));
+                const int rl = __ffs(bm[c]) - 1;
+                *o++ = (uint8_t)(((uint32_t)kCtxAGG << 1) | 1u);
+                *o++ = (uint8_t)(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl >> 1));
+                *o++ = (uint8_t)(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl & 1u));
                 // sign of the run's first significant sample
-                const uint64_t Nm = rl == 0 ? Gp : Fr[rl - 1];
-                const uint64_t Sm = rl < 3 ? Gr[rl + 1] : Gd;
-                uint32_t sw = bitat(westm(Fr[rl]), x), sn = bitat(Nm, x);
-                uint32_t se = bitat(eastm(Gr[rl]), x), ss = bitat(Sm, x);
-                uint32_t gw = x > 0 ? bitat(Sg[rl], x - 1) : 0u;
-                uint32_t gn = bitat(rl == 0 ? SgP : Sg[rl - 1], x);
-                uint32_t ge = x < 63 ? bitat(Sg[rl], x + 1) : 0u;
-                uint32_t gs = bitat(rl < 3 ? Sg[rl + 1] : SgD, x);
-                uint32_t lu = sign_index(sw, gw, sn, gn, se, ge, ss, gs);
-                e.push(((uint32_t)t.sc[lu] << 1) | (bitat(Sg[rl], x) ^ t.spb[lu]));
+                const uint32_t uf = rl == 0 ? wgp : wF[rl > 0 ? rl - 1 : 0], up = rl == 0 ? wgp : wG[rl > 0 ? rl - 1 : 0];
+                const uint32_t df = rl == 3 ? wgd : wF[rl < 3 ? rl + 1 : 3], dp = rl == 3 ? wgd : wG[rl < 3 ? rl + 1 : 3];
+                const uint32_t m8 = zc_index(uf, up, wF[rl], wG[rl], df, dp, c);
+                *o++ = (uint8_t)sign_symbol(t, m8, wsg[rl + 1], wsg[rl], wsg[rl + 2], c);
                 first = rl + 1;
               }
             }
-            for (int r = first; r < lim; ++r) {
-              if (!bitat(Cr[r], x)) continue;
-              const uint64_t Nr = r == 0 ? Gp : Fr[r - 1];
-              const uint64_t NEr = r == 0 ? Gp : Gr[r - 1];
-              const uint64_t Dr = r < 3 ? Gr[r + 1] : Gd;
-              const uint64_t DWr = r < 3 ? Fr[r + 1] : Gd;
-              emit_zc(e, t, x, bitat(Br[r], x), westm(Nr), Nr, eastm(NEr), westm(Fr[r]), eastm(Gr[r]),
-                      westm(DWr), Dr, eastm(Dr), Sg[r], r == 0 ? SgP : Sg[r - 1], r < 3 ? Sg[r + 1] : SgD,
-                      Sg[r]);
+            #pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              if (r < first || !((cm[c] >> r) & 1u)) continue;
+              const uint32_t uf = r == 0 ? wgp : wF[r > 0 ? r - 1 : 0], up = r == 0 ? wgp : wG[r > 0 ? r - 1 : 0];
+              const uint32_t df = r == 3 ? wgd : wF[r < 3 ? r + 1 : 3], dp = r == 3 ? wgd : wG[r < 3 ? r + 1 : 3];
+              const uint32_t m8 = zc_index(uf, up, wF[r], wG[r], df, dp, c);
+              const uint32_t bit = (bm[c] >> r) & 1u;
+              *o++ = (uint8_t)(((uint32_t)t.zc[m8] << 1) | bit);
+              if (bit) *o++ = (uint8_t)sign_symbol(t, m8, wsg[r + 1], wsg[r], wsg[r + 2], c);
             }
           }
-          flush_symbols(e, out, &pos, lane);
         }
         Gp = Fr[lim - 1];
       }
