@@ -90,7 +90,8 @@ struct jp2g_ctx {
   std::mutex mu;
   // device pools
   DevBuf px, ll0, ll1, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
-      hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym, stats;
+      hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym, stats, dwtargs,
+      dwtbases;
   // pinned host staging
   HostBuf hpx, hkeep, hoffsets, hbody, hres, hcount;
   bool timing = false;
@@ -222,80 +223,153 @@ void build_tables(const PagePlan& p, uint32_t block_base, uint32_t band_base, ui
   }
 }
 
-// Runs colour+DWT+quantisation for the page whose interleaved pixels are at
-// `d_px` on the device, filling the code-block slots from `block_base` on.
-int run_dwt(jp2g_ctx* c, const PagePlan& p, const uint8_t* d_px, uint32_t block_base) {
+// Arguments of decomposition level l (1 = first) of a page whose pixels are
+// at d_px; llA/llB are the page's two LL planes (level l writes its LL to
+// llA when l is odd, to llB when even, and reads the other).
+DwtLevelArgs level_args(const PagePlan& p, int l, const uint8_t* d_px, uint32_t block_base,
+                        int32_t* coef, void* llA, void* llB) {
+  DwtLevelArgs a{};
   const int L = p.levels;
-  size_t llw = (p.width + 1) / 2, llh = (p.height + 1) / 2;
-  size_t ll_elems = llw * llh * p.ncomp;
-  if (L >= 2) {
-    if (!reserve(c, c->ll0, ll_elems * 4) || !reserve(c, c->ll1, ll_elems * 4)) return kEncodeFailed;
+  const int res = L - l + 1;  // resolution whose detail bands this level makes
+  a.rw = p.ladder[res].first;
+  a.rh = p.ladder[res].second;
+  a.ncomp = p.ncomp;
+  a.mct = p.use_mct;
+  if (l == 1) {
+    a.from_pixels = 1;
+    a.px = d_px;
+    a.px_pitch = (size_t)p.width * p.ncomp;
+  } else {
+    a.src = (l - 1) % 2 ? llA : llB;
+    a.src_pitch = (size_t)p.ladder[res].first;
+    a.src_comp = a.src_pitch * (size_t)p.ladder[res].second;
   }
-  auto band_out = [&](DwtLevelArgs& a, int res) {
+  a.coef = coef;
+  a.cbw = p.cbw;
+  a.cbh = p.cbh;
+  auto band_out = [&](int r) {
     for (const BandGeom& g : p.bands) {
-      if (g.res != res) continue;
+      if (g.res != r) continue;
       DwtBandOut& o = a.band[g.comp][g.orient];
       o.first_block = block_base + g.first_block;
       o.ncbx = std::max(g.ncbx, 1);
       o.step = p.quants[g.quant].step_f32;
     }
   };
-  const void* src = nullptr;
-  size_t src_pitch = 0, src_comp = 0;
+  band_out(res);
+  if (l == L) {
+    a.ll = nullptr;
+    band_out(0);
+  } else {
+    a.ll = l % 2 ? llA : llB;
+    a.ll_pitch = (size_t)p.ladder[res - 1].first;
+    a.ll_comp = a.ll_pitch * (size_t)p.ladder[res - 1].second;
+  }
+  return a;
+}
+
+// Colour + DWT + quantisation of every page of a wave. Each level is one
+// launch over the tiles of all pages that have it (one per transform kind);
+// a page whose region at some level is under 2 samples wide or high, or that
+// has no decomposition level, takes the per-page kernel there.
+int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live) {
+  const size_t n = live.size();
+  std::vector<size_t> ll_off(n, 0);
+  size_t ll_total = 0;
+  int maxL = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const PagePlan& p = live[i]->plan;
+    maxL = std::max(maxL, p.levels);
+    if (p.levels >= 2) {
+      const size_t e = ((size_t)(p.width + 1) / 2) * ((p.height + 1) / 2) * p.ncomp;
+      ll_off[i] = ll_total;
+      ll_total += 2 * ((e + 63) & ~size_t(63));
+    }
+  }
+  if (ll_total > 0 && !reserve(c, c->ll0, ll_total * 4)) return kEncodeFailed;
+  int32_t* coef = dptr<int32_t>(c->coef);
+  auto page_px = [&](size_t i) {
+    return live[i]->dev_px ? live[i]->dev_px : dptr<uint8_t>(c->px) + live[i]->px_off;
+  };
   int launches = 0;
-  if (L == 0) {
+  // pages with no decomposition level: copy (and quantise) into blocks
+  for (size_t i = 0; i < n; ++i) {
+    const PagePlan& p = live[i]->plan;
+    if (p.levels != 0) continue;
     DwtLevelArgs a{};
     a.from_pixels = 1;
-    a.px = d_px;
+    a.px = page_px(i);
     a.px_pitch = (size_t)p.width * p.ncomp;
     a.mct = p.use_mct;
     a.ncomp = p.ncomp;
     a.rw = p.width;
     a.rh = p.height;
     a.no_transform = 1;
-    a.ll = nullptr;
-    a.coef = dptr<int32_t>(c->coef);
+    a.coef = coef;
     a.cbw = p.cbw;
     a.cbh = p.cbh;
-    band_out(a, 0);
+    for (const BandGeom& g : p.bands) {
+      DwtBandOut& o = a.band[g.comp][g.orient];
+      o.first_block = live[i]->block_base + g.first_block;
+      o.ncbx = std::max(g.ncbx, 1);
+      o.step = p.quants[g.quant].step_f32;
+    }
     launch_dwt_level(a, p.lossless, c->stream);
     ++launches;
   }
-  for (int l = 1; l <= L; ++l) {
-    DwtLevelArgs a{};
-    const int res = L - l + 1;  // resolution whose detail bands this level makes
-    a.rw = p.ladder[res].first;
-    a.rh = p.ladder[res].second;
-    a.ncomp = p.ncomp;
-    a.mct = p.use_mct;
-    if (l == 1) {
-      a.from_pixels = 1;
-      a.px = d_px;
-      a.px_pitch = (size_t)p.width * p.ncomp;
-    } else {
-      a.from_pixels = 0;
-      a.src = src;
-      a.src_pitch = src_pitch;
-      a.src_comp = src_comp;
+  struct Group {
+    size_t arg0, base0;
+    uint32_t npages, ntiles;
+    bool rev;
+  };
+  std::vector<DwtLevelArgs> args;
+  std::vector<uint32_t> bases;
+  std::vector<std::vector<Group>> groups(maxL + 1);
+  std::vector<std::vector<std::pair<DwtLevelArgs, bool>>> singles(maxL + 1);
+  for (int l = 1; l <= maxL; ++l)
+    for (int kind = 0; kind < 2; ++kind) {
+      const bool rev = kind == 0;
+      Group g{args.size(), bases.size(), 0, 0, rev};
+      for (size_t i = 0; i < n; ++i) {
+        const PagePlan& p = live[i]->plan;
+        if (p.levels < l || p.lossless != rev) continue;
+        int32_t* ll = dptr<int32_t>(c->ll0) + ll_off[i];
+        const size_t half = p.levels >= 2
+            ? (((size_t)(p.width + 1) / 2) * ((p.height + 1) / 2) * p.ncomp + 63) & ~size_t(63)
+            : 0;
+        DwtLevelArgs a = level_args(p, l, page_px(i), live[i]->block_base, coef, ll, ll + half);
+        if (a.rw >= 2 && a.rh >= 2) {
+          args.push_back(a);
+          bases.push_back(g.ntiles);
+          g.ntiles += dwt_tiles(a.rw, a.rh, a.ncomp);
+          ++g.npages;
+        } else {
+          singles[l].push_back({a, rev});
+        }
+      }
+      bases.push_back(g.ntiles);
+      if (g.npages > 0) groups[l].push_back(g);
     }
-    a.coef = dptr<int32_t>(c->coef);
-    a.cbw = p.cbw;
-    a.cbh = p.cbh;
-    band_out(a, res);
-    if (l == L) {
-      a.ll = nullptr;
-      band_out(a, 0);
-    } else {
-      DevBuf& dst = (l % 2) ? c->ll0 : c->ll1;
-      a.ll = dst.p;
-      a.ll_pitch = (size_t)p.ladder[res - 1].first;
-      a.ll_comp = a.ll_pitch * (size_t)p.ladder[res - 1].second;
-      src = a.ll;
-      src_pitch = a.ll_pitch;
-      src_comp = a.ll_comp;
+  if (!args.empty()) {
+    if (!reserve(c, c->dwtargs, args.size() * sizeof(DwtLevelArgs)) ||
+        !reserve(c, c->dwtbases, bases.size() * sizeof(uint32_t)) ||
+        !cuda_ok(c, cudaMemcpyAsync(c->dwtargs.p, args.data(), args.size() * sizeof(DwtLevelArgs),
+                                    cudaMemcpyHostToDevice, c->stream), "H2D level arguments") ||
+        !cuda_ok(c, cudaMemcpyAsync(c->dwtbases.p, bases.data(), bases.size() * sizeof(uint32_t),
+                                    cudaMemcpyHostToDevice, c->stream), "H2D tile bases"))
+      return kEncodeFailed;
+  }
+  const DwtLevelArgs* d_args = dptr<DwtLevelArgs>(c->dwtargs);
+  const uint32_t* d_bases = dptr<uint32_t>(c->dwtbases);
+  for (int l = 1; l <= maxL; ++l) {
+    for (const Group& g : groups[l]) {
+      launch_dwt_batch(d_args + g.arg0, d_bases + g.base0, g.npages, g.ntiles, g.rev, c->stream);
+      ++launches;
     }
-    launch_dwt_level(a, p.lossless, c->stream);
-    ++launches;
+    for (const auto& sa : singles[l]) {
+      launch_dwt_level(sa.first, sa.second, c->stream);
+      ++launches;
+    }
   }
   c->counters[5] += (uint64_t)launches;
   return kOk;
@@ -448,11 +522,8 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
                                   cudaMemcpyHostToDevice, c->stream), "H2D comps"))
     return kEncodeFailed;
   record(c, 1);
-  // ---- colour + DWT + quantisation, page by page ----
-  for (PageJob* j : live) {
-    const uint8_t* d_px = j->dev_px ? j->dev_px : dptr<uint8_t>(c->px) + j->px_off;
-    if (int rc = run_dwt(c, j->plan, d_px, j->block_base)) return rc;
-  }
+  // ---- colour + DWT + quantisation, one launch per level for the wave ----
+  if (int rc = run_dwt_wave(c, live)) return rc;
   record(c, 2);
   if (dbg && dbg->stop_after_dwt) {
     if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "DWT")) return kEncodeFailed;
@@ -723,7 +794,7 @@ void jp2g_destroy(jp2g_ctx* c) {
   DevBuf* bufs[] = {&c->px, &c->ll0, &c->ll1, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
-                    &c->itemrec, &c->sym, &c->stats};
+                    &c->itemrec, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   HostBuf* hb[] = {&c->hpx, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres, &c->hcount};

@@ -296,14 +296,58 @@ __device__ __forceinline__ void lift_regs(T (&x)[RN]) {
   }
 }
 
+// One value of the level's input: the page's pixels (level shift and
+// RCT/ICT applied) or the previous level's LL plane.
 template <bool REV>
-__global__ void __launch_bounds__(RT) dwt_tile_kernel(DwtLevelArgs a) {
+struct TileSrc {
   using T = typename Cfg<REV>::T;
-  __shared__ T s[RSH * RP];
-  const int comp = blockIdx.z;
-  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
-  const int rw = a.rw, rh = a.rh;
+  const uint8_t* px;
+  size_t px_pitch;
+  const T* ll;
+  size_t ll_pitch;
+  int ncomp, comp, mct, from_pixels;
+  __device__ __forceinline__ T at(int gx, int gy) const {
+    if (from_pixels) {
+      const uint8_t* row = px + (size_t)gy * px_pitch;
+      if (!mct) return (T)((int)row[(size_t)gx * ncomp + comp] - 128);
+      const uint8_t* q = row + (size_t)gx * 3;
+      const int r = (int)q[0] - 128, g = (int)q[1] - 128, b = (int)q[2] - 128;
+      if constexpr (REV) {  // RCT (src/simd/scalar.rs:173-195)
+        return (T)(comp == 0 ? ((r + 2 * g + b) >> 2) : (comp == 1 ? b - g : r - g));
+      } else {  // ICT (src/simd/scalar.rs:149-171), evaluated left to right
+        const float rf = (float)r, gf = (float)g, bf = (float)b;
+        if (comp == 0)
+          return __fadd_rn(__fadd_rn(__fmul_rn(0.299f, rf), __fmul_rn(0.587f, gf)), __fmul_rn(0.114f, bf));
+        if (comp == 1)
+          return __fadd_rn(__fadd_rn(__fmul_rn(-0.16875f, rf), __fmul_rn(-0.33126f, gf)), __fmul_rn(0.5f, bf));
+        return __fsub_rn(__fsub_rn(__fmul_rn(0.5f, rf), __fmul_rn(0.41869f, gf)), __fmul_rn(0.08131f, bf));
+      }
+    }
+    return ll[(size_t)gy * ll_pitch + gx];
+  }
+};
+
+// One tile of one level (see the comment above RT). The level's arguments
+// are read once into registers: the caller's copy may live in global memory.
+template <bool REV>
+__device__ __forceinline__ void dwt_tile(const DwtLevelArgs& args, int comp, int x0, int y0,
+                                         typename Cfg<REV>::T* s) {
+  using T = typename Cfg<REV>::T;
+  const int rw = args.rw, rh = args.rh;
   const int tid = threadIdx.x;
+  TileSrc<REV> src;
+  src.from_pixels = args.from_pixels;
+  src.px = args.px;
+  src.px_pitch = args.px_pitch;
+  src.ncomp = args.ncomp;
+  src.comp = comp;
+  src.mct = args.mct;
+  src.ll = reinterpret_cast<const T*>(args.src) + (size_t)comp * args.src_comp;
+  src.ll_pitch = args.src_pitch;
+  T* const ll_out = args.ll ? reinterpret_cast<T*>(args.ll) + (size_t)comp * args.ll_comp : nullptr;
+  const size_t ll_pitch = args.ll_pitch;
+  int32_t* const coef = args.coef;
+  const int cbw = args.cbw, cbh = args.cbh;
 
   // ---- load tile + halo (mirrored at the region borders) ----
   {
@@ -315,7 +359,7 @@ __global__ void __launch_bounds__(RT) dwt_tile_kernel(DwtLevelArgs a) {
       for (int lx = tx; lx < RSW; lx += 32) {
         int gx = x0 - RH + lx;
         if (!inner_x && (unsigned)gx >= (unsigned)rw) gx = sym(gx, rw);
-        s[ly * RP + lx] = load_sample<REV>(a, comp, gx, gy);
+        s[ly * RP + lx] = src.at(gx, gy);
       }
     }
   }
@@ -364,31 +408,82 @@ __global__ void __launch_bounds__(RT) dwt_tile_kernel(DwtLevelArgs a) {
   }
   __syncthreads();
 
-  // ---- epilogue: subbands in row order, quantised into code-block slots ----
-  const int cbs = __ffs(a.cbw) - 1, cbhs = __ffs(a.cbh) - 1;
+  // ---- epilogue: each subband's 64 x 32 part, rows in order ----
+  const int cbs = __ffs(cbw) - 1, cbhs = __ffs(cbh) - 1;
   const int u0 = x0 >> 1, v0 = y0 >> 1;
-  const int bw_lo = (rw + 1) >> 1, bw_hi = rw >> 1, bh_lo = (rh + 1) >> 1, bh_hi = rh >> 1;
-  for (int idx = tid; idx < 4 * 32 * 64; idx += RT) {
-    const int band = idx >> 11, rr = (idx >> 6) & 31, cc = idx & 63;  // band: LL, HL, LH, HH
-    const int u = u0 + cc, v = v0 + rr;
-    const int bw = (band & 1) ? bw_hi : bw_lo, bh = (band & 2) ? bh_hi : bh_lo;
-    if (u >= bw || v >= bh) continue;
-    T val = s[(RH + 2 * rr + (band >> 1)) * RP + RH + 2 * cc + (band & 1)];
-    if constexpr (!REV) val = __fmul_rn(val, (band & 1) ? kK : kInvK);  // columns: 1/K even, K odd
-    if (band == 0 && a.ll != nullptr) {
-      reinterpret_cast<T*>(a.ll)[(size_t)comp * a.ll_comp + (size_t)v * a.ll_pitch + u] = val;
+  #pragma unroll 1
+  for (int band = 0; band < 4; ++band) {  // LL, HL, LH, HH
+    const int bw = (band & 1) ? rw >> 1 : (rw + 1) >> 1;
+    const int bh = (band & 2) ? rh >> 1 : (rh + 1) >> 1;
+    const int cols = min(64, bw - u0), rows = min(32, bh - v0);
+    if (cols <= 0 || rows <= 0) continue;
+    const T* sb = s + (RH + (band >> 1)) * RP + RH + (band & 1);
+    const float cscale = (band & 1) ? kK : kInvK;  // columns: 1/K even, K odd (9/7)
+    if (band == 0 && ll_out != nullptr) {
+      for (int idx = tid; idx < 32 * 64; idx += RT) {
+        const int rr = idx >> 6, cc = idx & 63;
+        if (rr >= rows || cc >= cols) continue;
+        T val = sb[2 * rr * RP + 2 * cc];
+        if constexpr (!REV) val = __fmul_rn(val, cscale);
+        ll_out[(size_t)(v0 + rr) * ll_pitch + u0 + cc] = val;
+      }
       continue;
     }
-    const DwtBandOut& bo = a.band[comp][band];
-    const uint32_t blk = bo.first_block + (uint32_t)(v >> cbhs) * bo.ncbx + (uint32_t)(u >> cbs);
-    int32_t qv;
-    if constexpr (REV) qv = val;
-    else qv = quantize(val, bo.step);
-    a.coef[((size_t)blk << (cbs + cbhs)) + ((size_t)(v & (a.cbh - 1)) << cbs) + (u & (a.cbw - 1))] = qv;
+    const DwtBandOut bo = args.band[comp][band];
+    for (int idx = tid; idx < 32 * 64; idx += RT) {
+      const int rr = idx >> 6, cc = idx & 63;
+      if (rr >= rows || cc >= cols) continue;
+      T val = sb[2 * rr * RP + 2 * cc];
+      const int u = u0 + cc, v = v0 + rr;
+      const uint32_t blk = bo.first_block + (uint32_t)(v >> cbhs) * bo.ncbx + (uint32_t)(u >> cbs);
+      int32_t qv;
+      if constexpr (REV) qv = val;
+      else qv = quantize(__fmul_rn(val, cscale), bo.step);
+      coef[((size_t)blk << (cbs + cbhs)) + ((size_t)(v & (cbh - 1)) << cbs) + (u & (cbw - 1))] = qv;
+    }
   }
 }
 
+template <bool REV>
+__global__ void __launch_bounds__(RT) dwt_tile_kernel(DwtLevelArgs a) {
+  __shared__ typename Cfg<REV>::T s[RSH * RP];
+  dwt_tile<REV>(a, blockIdx.z, blockIdx.x * TW, blockIdx.y * TH, s);
+}
+
+// Flat tile list over many pages: the CTA finds its page by binary search
+// over the tile bases, then its component and tile position.
+template <bool REV>
+__global__ void __launch_bounds__(RT) dwt_batch_kernel(const DwtLevelArgs* __restrict__ args,
+                                                       const uint32_t* __restrict__ tile_base,
+                                                       uint32_t npages) {
+  __shared__ typename Cfg<REV>::T s[RSH * RP];
+  const uint32_t t = blockIdx.x;
+  uint32_t lo = 0, hi = npages;  // tile_base[lo] <= t < tile_base[hi]
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (tile_base[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  const DwtLevelArgs& a = args[lo];
+  const uint32_t local = t - tile_base[lo];
+  const uint32_t ntx = (uint32_t)(a.rw + TW - 1) / TW, nty = (uint32_t)(a.rh + TH - 1) / TH;
+  const uint32_t comp = local / (ntx * nty), rem = local - comp * ntx * nty;
+  const uint32_t ty = rem / ntx, tx = rem - ty * ntx;
+  dwt_tile<REV>(a, (int)comp, (int)tx * TW, (int)ty * TH, s);
+}
+
 }  // namespace
+
+uint32_t dwt_tiles(int rw, int rh, int ncomp) {
+  return (uint32_t)((rw + TW - 1) / TW) * (uint32_t)((rh + TH - 1) / TH) * (uint32_t)ncomp;
+}
+
+void launch_dwt_batch(const DwtLevelArgs* d_args, const uint32_t* d_tile_base, uint32_t npages,
+                      uint32_t ntiles, bool reversible, cudaStream_t st) {
+  if (npages == 0 || ntiles == 0) return;
+  if (reversible) dwt_batch_kernel<true><<<ntiles, RT, 0, st>>>(d_args, d_tile_base, npages);
+  else dwt_batch_kernel<false><<<ntiles, RT, 0, st>>>(d_args, d_tile_base, npages);
+}
 
 void launch_dwt_level(const DwtLevelArgs& a, bool reversible, cudaStream_t st) {
   dim3 grid((a.rw + TW - 1) / TW, (a.rh + TH - 1) / TH, a.ncomp);

@@ -35,6 +35,14 @@ struct DwtLevelArgs {
 
 void launch_dwt_level(const DwtLevelArgs& a, bool reversible, cudaStream_t st);
 
+// One level of many pages in one launch: d_args[i] describes page i's level
+// (region at least 2x2), d_tile_base[i] its first tile in the flat tile
+// list (npages + 1 entries, d_tile_base[npages] = the tile count).
+void launch_dwt_batch(const DwtLevelArgs* d_args, const uint32_t* d_tile_base, uint32_t npages,
+                      uint32_t ntiles, bool reversible, cudaStream_t st);
+// Tiles of one page's level in the flat tile list.
+uint32_t dwt_tiles(int rw, int rh, int ncomp);
+
 struct T1Args {
   const BlockDesc* blocks;
   uint32_t nblocks;
