@@ -157,6 +157,7 @@ def _rgb_pages(n, seed0):
 
 
 UNEVEN_DIMS = [(1275, 1650), (2550, 3300), (3400, 4400), (5100, 6600)]
+SERVE_P99_SLO_MS = 1000.0
 
 
 def _uneven_page(seed):
@@ -303,16 +304,19 @@ def bench_served(jl, local, args):
         mpix = sum(r["w"] * r["h"] for r in reqs) / 1e6
         lat_ms = np.array(lat) * 1e3
         rows.append({"offered_pages_per_s": rate, "requests": n, "achieved_pages_per_s": n / wall,
+                     "arrival_window_s": float(sum(gaps)), "wall_s": wall,
                      "mpix_per_s": mpix / wall, "p50_ms": float(np.percentile(lat_ms, 50)),
                      "p99_ms": float(np.percentile(lat_ms, 99)),
                      "p99_9_ms": float(np.percentile(lat_ms, 99.9))})
     eng.close()
-    sustained = [r for r in rows if r["achieved_pages_per_s"] >= 0.95 * r["offered_pages_per_s"]]
+    # sustained: the queue does not build up, i.e. p99 latency stays under
+    # the 1 s objective over the whole arrival window
+    sustained = [r for r in rows if r["p99_ms"] <= SERVE_P99_SLO_MS]
     return {"workload": "Poisson arrivals (seed 42), 70% uneven pages drawn from a pool of "
                         f"{args.serve_pool} (seeds 3000+i) / 30% 256x256 gray q60 thumbnails, JP2, "
                         f"{args.serve_seconds} s per offered rate, 40 GB device budget, "
                         "latency = submit -> result on the host",
-            "rates": rows,
+            "rates": rows, "p99_objective_ms": SERVE_P99_SLO_MS,
             "highest_sustained_pages_per_s": max((r["offered_pages_per_s"] for r in sustained), default=None)}
 
 
@@ -328,7 +332,7 @@ def main():
     ap.add_argument("--batch-pages", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--uneven-pages", type=int, default=64)
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[50, 100, 200, 400])
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[50, 100, 150, 200, 300, 400])
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--serve-pool", type=int, default=12)
     args = ap.parse_args()

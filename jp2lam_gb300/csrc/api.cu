@@ -91,7 +91,7 @@ struct jp2g_ctx {
   // device pools
   DevBuf px, ll0, ll1, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
       hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym, stats, dwtargs,
-      dwtbases;
+      dwtbases, mqorder, mqscratch;
   // pinned host staging
   HostBuf hpx, hkeep, hoffsets, hbody, hres, hcount;
   bool timing = false;
@@ -564,8 +564,19 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
   record(c, kEvAnalyzeEnd);
   launch_t1_model(ta, c->num_sms, c->stream);
   record(c, kEvModelEnd);
-  launch_t1_mq(ta, c->num_sms, (int)c->opt[JP2G_OPT_MQ_BLOCKS_PER_WARP], c->stream);
-  c->counters[5] += 5 + (nb > 1024 ? 1 : 0);
+  // Several blocks per warp: code them heaviest first, so that each warp's
+  // lanes carry similar symbol counts.
+  const int bpw = mq_blocks_per_warp(ta, c->num_sms, (int)c->opt[JP2G_OPT_MQ_BLOCKS_PER_WARP]);
+  int order_launches = 0;
+  if (bpw > 1) {
+    if (!reserve(c, c->mqorder, (size_t)nb * 4) || !reserve(c, c->mqscratch, ((size_t)nb + 2048) * 4))
+      return kEncodeFailed;
+    launch_mq_order(ta, dptr<uint32_t>(c->mqorder), dptr<uint32_t>(c->mqscratch), c->stream);
+    ta.mq_order = dptr<uint32_t>(c->mqorder);
+    order_launches = 3;
+  }
+  launch_t1_mq(ta, c->num_sms, bpw, c->stream);
+  c->counters[5] += 5 + (nb > 1024 ? 1 : 0) + order_launches;
   record(c, 3);
   // ---- PCRD ----
   PcrdArgs pa{};
@@ -794,7 +805,8 @@ void jp2g_destroy(jp2g_ctx* c) {
   DevBuf* bufs[] = {&c->px, &c->ll0, &c->ll1, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
-                    &c->itemrec, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases};
+                    &c->itemrec, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases, &c->mqorder,
+                    &c->mqscratch};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   HostBuf* hb[] = {&c->hpx, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres, &c->hcount};

@@ -61,6 +61,7 @@ struct T1Args {
   uint8_t* sym;          // per item: a slot of sym_slot symbol bytes
   uint32_t sym_slot;
   unsigned long long* sym_count;  // total MQ symbols coded (statistics)
+  const uint32_t* mq_order;       // MQ processing order of the blocks, or null (work-list order)
 };
 
 void launch_t1_analyze(const T1Args& a, cudaStream_t st);
@@ -68,6 +69,11 @@ void launch_t1_items(const T1Args& a, cudaStream_t st);
 void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st);
 // bpw: code-blocks per warp, 1..32, or 0 for automatic.
 void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st);
+// Code-blocks per warp that launch_t1_mq uses for `bpw` (0 = automatic).
+int mq_blocks_per_warp(const T1Args& a, int num_sms, int bpw);
+// Orders the blocks by their MQ symbol count, largest first (counting sort
+// on 1024 buckets), into order[nblocks]. scratch: nblocks + 2048 words.
+void launch_mq_order(const T1Args& a, uint32_t* order, uint32_t* scratch, cudaStream_t st);
 
 // Exclusive prefix sum of n uint32 values read with a stride of `stride`
 // words: out[i] = sum of in[0..i), out[n] = total. `scratch` holds

@@ -152,6 +152,15 @@ __device__ __forceinline__ uint32_t sign_symbol(const ModelTables& t, uint32_t m
   return ((uint32_t)t.sc[lu] << 1) | (((g >> (c + 1)) & 1u) ^ t.spb[lu]);
 }
 
+// a[i] for a runtime i without indexing a register array (which would move
+// the array to local memory).
+__device__ __forceinline__ uint32_t pick4(const uint32_t (&a)[4], int i) {
+  return i < 2 ? (i == 0 ? a[0] : a[1]) : (i == 2 ? a[2] : a[3]);
+}
+__device__ __forceinline__ uint32_t pick6(const uint32_t (&a)[6], int i) {
+  return i < 3 ? (i == 0 ? a[0] : (i == 1 ? a[1] : a[2])) : (i == 3 ? a[3] : (i == 4 ? a[4] : a[5]));
+}
+
 // Exclusive prefix of v over the warp's lanes; *total = the warp's sum.
 __device__ __forceinline__ uint32_t warp_offset(uint32_t v, int lane, uint32_t* total) {
   uint32_t x = v;
@@ -164,7 +173,7 @@ __device__ __forceinline__ uint32_t warp_offset(uint32_t v, int lane, uint32_t* 
   return x - v;
 }
 
-__global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
+__global__ void __launch_bounds__(kModelWarps * 32, 3) t1_model_kernel(T1Args a) {
   __shared__ ModelSmem sm_all[kModelWarps];
   __shared__ uint8_t s_zc[4 * 512];
   __shared__ uint8_t s_sc[256];
@@ -276,7 +285,7 @@ __global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
           uint8_t* o = out + pos + warp_offset(cnt, lane, &total);
           pos += total;
           n_sp += total;
-          #pragma unroll
+          #pragma unroll 1
           for (int c = 0; c < 2; ++c) {
             #pragma unroll
             for (int r = 0; r < 4; ++r) {
@@ -313,7 +322,7 @@ __global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
         uint8_t* o = out + pos + warp_offset(cnt, lane, &total);
         pos += total;
         n_mr += total;
-        #pragma unroll
+        #pragma unroll 1
         for (int c = 0; c < 2; ++c) {
           #pragma unroll
           for (int r = 0; r < 4; ++r) {
@@ -350,8 +359,11 @@ __global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
         const uint64_t Gd = lim == 4 && k + 4 < h ? (s.S[k + 5] | s.N[k + 5]) : 0;  // next stripe, pre-CL
         const uint64_t SgP = s.Sn[k], SgD = s.Sn[k + 5];
         ns_cl += __popcll(Qr[0]) + __popcll(Qr[1]) + __popcll(Qr[2]) + __popcll(Qr[3]);
-        if (lane == 0)
-          for (int r = 0; r < lim; ++r) s.Q[k + r + 1] = Qr[r];
+        if (lane == 0) {
+          #pragma unroll
+          for (int r = 0; r < 4; ++r)
+            if (r < lim) s.Q[k + r + 1] = Qr[r];
+        }
         // run-length eligibility of each column (flags.rs:219-235)
         uint64_t clean = 0;
         if (lim == 4) {
@@ -374,64 +386,65 @@ __global__ void __launch_bounds__(kModelWarps * 32) t1_model_kernel(T1Args a) {
           #pragma unroll
           for (int r = 0; r < 4; ++r) wsg[r + 1] = win4(Sg[r], sh);
           wsg[5] = win4(SgD, sh);
-          // per column: candidate rows, their bits, run-mode eligibility
-          uint32_t cm[2], bm[2], cnt = 0;
+          // per column: candidate rows (4-bit), their bits, run-mode eligibility
+          auto col_bits = [&](const uint32_t (&wv)[4], int c) {
+            uint32_t m = 0;
+            #pragma unroll
+            for (int r = 0; r < 4; ++r) m |= ((wv[r] >> (c + 1)) & 1u) << r;
+            return m;
+          };
+          uint32_t cnt = 0;
           #pragma unroll
           for (int c = 0; c < 2; ++c) {
-            cm[c] = 0;
-            bm[c] = 0;
-            #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-              cm[c] |= ((wC[r] >> (c + 1)) & 1u) << r;
-              bm[c] |= ((wB[r] >> (c + 1)) & 1u) << r;
-            }
+            const uint32_t cmc = col_bits(wC, c), bmc = col_bits(wB, c);
             if ((wcl >> (c + 1)) & 1u) {
-              if (bm[c] == 0) {
+              if (bmc == 0) {
                 cnt += 1;
               } else {
-                const uint32_t after = 0xfu & ~((2u << (__ffs(bm[c]) - 1)) - 1u);
-                cnt += 4 + __popc(after) + __popc(bm[c] & after);
+                const uint32_t after = 0xfu & ~((2u << (__ffs(bmc) - 1)) - 1u);
+                cnt += 4 + __popc(after) + __popc(bmc & after);
               }
             } else {
-              cnt += __popc(cm[c]) + __popc(cm[c] & bm[c]);
+              cnt += __popc(cmc) + __popc(cmc & bmc);
             }
           }
           uint32_t total;
           uint8_t* o = out + pos + warp_offset(cnt, lane, &total);
           pos += total;
-          #pragma unroll
+          #pragma unroll 1
           for (int c = 0; c < 2; ++c) {
+            const uint32_t cmc = col_bits(wC, c), bmc = col_bits(wB, c);
             int first = 0;
             if ((wcl >> (c + 1)) & 1u) {
-              if (bm[c] == 0) {
+              if (bmc == 0) {
                 *o++ = (uint8_t)((uint32_t)kCtxAGG << 1);
                 first = 4;
               } else {
-                const int rl = __ffs(bm[c]) - 1;
+                const int rl = __ffs(bmc) - 1;
                 *o++ = (uint8_t)(((uint32_t)kCtxAGG << 1) | 1u);
                 *o++ = (uint8_t)(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl >> 1));
                 *o++ = (uint8_t)(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl & 1u));
                 // sign of the run's first significant sample
-                const uint32_t uf = rl == 0 ? wgp : wF[rl > 0 ? rl - 1 : 0], up = rl == 0 ? wgp : wG[rl > 0 ? rl - 1 : 0];
-                const uint32_t df = rl == 3 ? wgd : wF[rl < 3 ? rl + 1 : 3], dp = rl == 3 ? wgd : wG[rl < 3 ? rl + 1 : 3];
-                const uint32_t m8 = zc_index(uf, up, wF[rl], wG[rl], df, dp, c);
-                *o++ = (uint8_t)sign_symbol(t, m8, wsg[rl + 1], wsg[rl], wsg[rl + 2], c);
+                const uint32_t uf = rl == 0 ? wgp : pick4(wF, rl - 1), up = rl == 0 ? wgp : pick4(wG, rl - 1);
+                const uint32_t df = rl == 3 ? wgd : pick4(wF, rl + 1), dp = rl == 3 ? wgd : pick4(wG, rl + 1);
+                const uint32_t m8 = zc_index(uf, up, pick4(wF, rl), pick4(wG, rl), df, dp, c);
+                *o++ = (uint8_t)sign_symbol(t, m8, pick6(wsg, rl + 1), pick6(wsg, rl), pick6(wsg, rl + 2), c);
                 first = rl + 1;
               }
             }
             #pragma unroll
             for (int r = 0; r < 4; ++r) {
-              if (r < first || !((cm[c] >> r) & 1u)) continue;
+              if (r < first || !((cmc >> r) & 1u)) continue;
               const uint32_t uf = r == 0 ? wgp : wF[r > 0 ? r - 1 : 0], up = r == 0 ? wgp : wG[r > 0 ? r - 1 : 0];
               const uint32_t df = r == 3 ? wgd : wF[r < 3 ? r + 1 : 3], dp = r == 3 ? wgd : wG[r < 3 ? r + 1 : 3];
               const uint32_t m8 = zc_index(uf, up, wF[r], wG[r], df, dp, c);
-              const uint32_t bit = (bm[c] >> r) & 1u;
+              const uint32_t bit = (bmc >> r) & 1u;
               *o++ = (uint8_t)(((uint32_t)t.zc[m8] << 1) | bit);
               if (bit) *o++ = (uint8_t)sign_symbol(t, m8, wsg[r + 1], wsg[r], wsg[r + 2], c);
             }
           }
         }
-        Gp = Fr[lim - 1];
+        Gp = lim == 4 ? Fr[3] : (lim == 3 ? Fr[2] : (lim == 2 ? Fr[1] : Fr[0]));
       }
       if (lane == 0) {
         ItemRec rec;
@@ -588,8 +601,9 @@ __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw)
   const int wid = threadIdx.x >> 5;
   if (lane >= bpw) return;
   uint2* ce = &ce_all[wid][lane];  // context c at ce[32 * c]
-  const uint32_t b = (blockIdx.x * kMqWarps + wid) * (uint32_t)bpw + (uint32_t)lane;
-  if (b >= a.nblocks) return;
+  const uint32_t slot = (blockIdx.x * kMqWarps + wid) * (uint32_t)bpw + (uint32_t)lane;
+  if (slot >= a.nblocks) return;
+  const uint32_t b = a.mq_order ? a.mq_order[slot] : slot;
   BlockOut o = a.res[b];
   const int mbp = o.status ? 0 : o.mbp;
   if (mbp == 0) return;
@@ -688,13 +702,85 @@ void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st) {
   t1_model_kernel<<<need < cap ? need : cap, kModelWarps * 32, 0, st>>>(a);
 }
 
-void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st) {
-  if (a.nblocks == 0) return;
+int mq_blocks_per_warp(const T1Args& a, int num_sms, int bpw) {
   // Automatic: one block per warp while that keeps at most 48 warps per SM,
   // 32 per warp beyond that.
   if (bpw <= 0 || bpw > 32) bpw = a.nblocks <= (uint32_t)num_sms * 48u ? 1 : 32;
+  return bpw;
+}
+
+void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st) {
+  if (a.nblocks == 0) return;
+  bpw = mq_blocks_per_warp(a, num_sms, bpw);
   const uint32_t per_cta = (uint32_t)bpw * kMqWarps;
   t1_mq_kernel<<<(a.nblocks + per_cta - 1) / per_cta, kMqWarps * 32, 0, st>>>(a, bpw);
+}
+
+namespace {
+constexpr uint32_t kOrderBuckets = 1024;
+
+// Bucket of a block: its MQ symbol count / 64, clamped, reversed so that
+// bucket 0 holds the largest blocks.
+__device__ __forceinline__ uint32_t order_bucket(const T1Args& a, uint32_t b) {
+  const uint32_t i0 = a.plane_base[b], i1 = a.plane_base[b + 1];
+  uint32_t n = 0;
+  for (uint32_t i = i0; i < i1; ++i) {
+    const ItemRec r = a.item_rec[i];
+    n += r.n_sp + r.n_mr + r.n_cl;
+  }
+  const uint32_t k = min(n >> 6, kOrderBuckets - 1);
+  return kOrderBuckets - 1 - k;
+}
+
+__global__ void order_hist_kernel(T1Args a, uint32_t* key, uint32_t* hist) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.nblocks) return;
+  const uint32_t k = order_bucket(a, b);
+  key[b] = k;
+  atomicAdd(hist + k, 1u);
+}
+
+// One CTA of 1024 threads: exclusive scan of the bucket counts into cursors.
+__global__ void order_scan_kernel(const uint32_t* hist, uint32_t* cursor) {
+  __shared__ uint32_t warp_tot[32];
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const uint32_t v = hist[t];
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t y = warp_tot[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t z = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += z;
+    }
+    warp_tot[lane] = y;
+  }
+  __syncthreads();
+  cursor[t] = x - v + (wid > 0 ? warp_tot[wid - 1] : 0u);
+}
+
+__global__ void order_scatter_kernel(uint32_t n, const uint32_t* key, uint32_t* cursor, uint32_t* order) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  order[atomicAdd(cursor + key[b], 1u)] = b;
+}
+}  // namespace
+
+void launch_mq_order(const T1Args& a, uint32_t* order, uint32_t* scratch, cudaStream_t st) {
+  if (a.nblocks == 0) return;
+  uint32_t* hist = scratch;
+  uint32_t* cursor = scratch + kOrderBuckets;
+  uint32_t* key = scratch + 2 * kOrderBuckets;
+  cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(uint32_t), st);
+  const uint32_t g = (a.nblocks + 255) / 256;
+  order_hist_kernel<<<g, 256, 0, st>>>(a, key, hist);
+  order_scan_kernel<<<1, kOrderBuckets, 0, st>>>(hist, cursor);
+  order_scatter_kernel<<<g, 256, 0, st>>>(a.nblocks, key, cursor, order);
 }
 
 }  // namespace jp2g
