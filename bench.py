@@ -309,9 +309,10 @@ def bench_served(jl, local, args):
                      "p99_ms": float(np.percentile(lat_ms, 99)),
                      "p99_9_ms": float(np.percentile(lat_ms, 99.9))})
     eng.close()
-    # sustained: the queue does not build up, i.e. p99 latency stays under
-    # the 1 s objective over the whole arrival window
-    sustained = [r for r in rows if r["p99_ms"] <= SERVE_P99_SLO_MS]
+    # sustained: completions keep up with arrivals (>= 90% of the offered
+    # rate, the drain included) and p99 latency stays under the objective
+    sustained = [r for r in rows
+                 if r["p99_ms"] <= SERVE_P99_SLO_MS and r["achieved_pages_per_s"] >= 0.9 * r["offered_pages_per_s"]]
     return {"workload": "Poisson arrivals (seed 42), 70% uneven pages drawn from a pool of "
                         f"{args.serve_pool} (seeds 3000+i) / 30% 256x256 gray q60 thumbnails, JP2, "
                         f"{args.serve_seconds} s per offered rate, 40 GB device budget, "
@@ -332,7 +333,7 @@ def main():
     ap.add_argument("--batch-pages", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--uneven-pages", type=int, default=64)
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[50, 100, 150, 200, 300, 400])
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[50, 100, 200, 250, 300, 350, 400])
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--serve-pool", type=int, default=12)
     args = ap.parse_args()

@@ -86,8 +86,9 @@ struct jp2g_ctx {
   cudaStream_t stream = nullptr;
   uint64_t budget = 0;
   uint64_t allocated = 0;
-  std::string err;
-  std::mutex mu;
+  std::string err;  // guarded by errmu
+  std::mutex errmu;
+  std::mutex mu;    // device pools and stream: one wave (or encode) at a time
   // device pools
   DevBuf px, ll0, ll1, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
       hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym, stats, dwtargs,
@@ -114,14 +115,24 @@ struct jp2g_ctx {
 
 namespace {
 
-int set_err(jp2g_ctx* c, int code, const std::string& m) {
+void set_msg(jp2g_ctx* c, const std::string& m) {
+  std::lock_guard<std::mutex> lk(c->errmu);
   c->err = m;
+}
+
+std::string get_msg(jp2g_ctx* c) {
+  std::lock_guard<std::mutex> lk(c->errmu);
+  return c->err;
+}
+
+int set_err(jp2g_ctx* c, int code, const std::string& m) {
+  set_msg(c, m);
   return code;
 }
 
 bool cuda_ok(jp2g_ctx* c, cudaError_t e, const char* what) {
   if (e == cudaSuccess) return true;
-  c->err = std::string(what) + ": " + cudaGetErrorString(e);
+  set_msg(c, std::string(what) + ": " + cudaGetErrorString(e));
   return false;
 }
 
@@ -130,7 +141,7 @@ bool reserve(jp2g_ctx* c, DevBuf& b, size_t bytes) {
   size_t want = std::max(bytes, b.cap + b.cap / 2);
   want = (want + 255) & ~size_t(255);
   if (c->budget && c->allocated - b.cap + want > c->budget) {
-    c->err = "device memory budget exhausted (" + std::to_string(c->budget) + " bytes)";
+    set_msg(c, "device memory budget exhausted (" + std::to_string(c->budget) + " bytes)");
     return false;
   }
   if (b.p) cudaFree(b.p);
@@ -937,7 +948,7 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
       }
     } else if (first_fail == JP2G_OK) {
       first_fail = jobs[i].status;
-      c->err = "page " + std::to_string(i) + ": " + jobs[i].err;
+      set_msg(c, "page " + std::to_string(i) + ": " + jobs[i].err);
     }
   }
   return first_fail;
@@ -974,7 +985,7 @@ void worker_loop(jp2g_ctx* c) {
     {
       std::lock_guard<std::mutex> lk(c->mu);
       rc = run_wave(c, jobs.data(), jobs.size(), nullptr);
-      if (rc != JP2G_OK) err = c->err;
+      if (rc != JP2G_OK) err = get_msg(c);
     }
     if (rc != JP2G_OK)
       for (PageJob* j : jobs) {
@@ -1014,18 +1025,13 @@ void finisher_loop(jp2g_ctx* c) {
 
 int jp2g_submit(jp2g_ctx* c, const jp2g_request* req, uint64_t* ticket) {
   if (!c) return JP2G_INVALID_INPUT;
-  if (!req || !ticket) {
-    std::lock_guard<std::mutex> lk(c->mu);
-    return set_err(c, JP2G_INVALID_INPUT, "null request or ticket pointer");
-  }
+  if (!req || !ticket) return set_err(c, JP2G_INVALID_INPUT, "null request or ticket pointer");
   auto t = std::make_shared<Ticket>();
   job_from_request(*req, &t->job);
   Failure f{};
   if (!build_plan(t->job.w, t->job.h, (int)t->job.ncomp, t->job.quality, t->job.format, &t->job.plan, &f) ||
-      !req->px) {
-    std::lock_guard<std::mutex> lk(c->mu);
+      !req->px)
     return set_err(c, req->px ? f.code : JP2G_INVALID_INPUT, req->px ? f.msg : "pixel pointer is null");
-  }
   {
     std::lock_guard<std::mutex> lk(c->qmu);
     if (!c->worker.joinable()) {
@@ -1043,17 +1049,13 @@ int jp2g_submit(jp2g_ctx* c, const jp2g_request* req, uint64_t* ticket) {
 
 int jp2g_poll(jp2g_ctx* c, uint64_t ticket, uint8_t** out, size_t* out_len, int timeout_ms) {
   if (!c) return JP2G_INVALID_INPUT;
-  if (!out || !out_len) {
-    std::lock_guard<std::mutex> lk(c->mu);
-    return set_err(c, JP2G_INVALID_INPUT, "output pointer is null");
-  }
+  if (!out || !out_len) return set_err(c, JP2G_INVALID_INPUT, "output pointer is null");
   std::shared_ptr<Ticket> t;
   {
     std::unique_lock<std::mutex> lk(c->qmu);
     auto it = c->tickets.find(ticket);
     if (it == c->tickets.end()) {
       lk.unlock();
-      std::lock_guard<std::mutex> g(c->mu);
       return set_err(c, JP2G_INVALID_INPUT, "unknown ticket " + std::to_string(ticket));
     }
     t = it->second;
@@ -1062,7 +1064,8 @@ int jp2g_poll(jp2g_ctx* c, uint64_t ticket, uint8_t** out, size_t* out_len, int 
     else if (!c->dcv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return JP2G_PENDING;
     c->tickets.erase(ticket);
   }
-  std::lock_guard<std::mutex> g(c->mu);
+  // the result is the ticket's own; the engine mutex (held by the worker
+  // for the whole device phase of a wave) is not needed
   if (t->job.status != JP2G_OK) return set_err(c, t->job.status, t->job.err);
   return finish_output(c, JP2G_OK, t->job.out, out, out_len);
 }
