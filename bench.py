@@ -329,6 +329,8 @@ def main():
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--only-batch", action="store_true",
+                    help="run only the batched leg (for profiling); prints its object")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-pages", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=3)
@@ -384,6 +386,11 @@ def main():
         times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
         return times, stages, outs
 
+    if args.only_batch:
+        eng.set_timing(True)
+        print(json.dumps(bench_batched(eng, stream, torch, f"cuda:{local}", args)), flush=True)
+        eng.close()
+        return
     dev_fn = lambda: eng.encode_device(d_px.data_ptr(), W, H, NCOMP, QUALITY, FMT)
     host_fn = lambda: eng.encode(px, W, H, NCOMP, QUALITY, FMT)
     for _ in range(args.warmup):
@@ -416,29 +423,40 @@ def main():
     st_mean = {k: float(np.mean([s[k] for s in dev_st])) for k in keys}
     peaks = _peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    # DWT+colour+quantisation: 5 algorithmic bytes per component-sample
-    # (1 B pixel read + 4 B int32 coefficient written).
+    # Algorithmic bytes per launch (one page per step), over the launch's
+    # CUDA-event time on the engine's stream:
+    #  DWT + colour + quantisation: 5 B per component-sample (1 B pixel read,
+    #    4 B int32 coefficient written), all levels together;
+    #  Tier-1 modelling: 4 B per coefficient per modelled bit-plane read
+    #    (counter 6) + 1 B per MQ symbol written (counter 7);
+    #  MQ coding: 1 B per symbol read + the payload bytes written (counter 3).
     dwt_bytes = 5.0 * W * H * NCOMP
-    dwt_gbs = dwt_bytes / (st_mean["dwt"] / 1e3) / 1e9 if st_mean["dwt"] > 0 else None
-    # Tier-1: 4 B per coefficient read + compressed bytes written.
-    t1_bytes = 4.0 * W * H * NCOMP + counters[3]
-    t1_gbs = t1_bytes / (st_mean["tier1"] / 1e3) / 1e9 if st_mean["tier1"] > 0 else None
-    dominant = max(("dwt", "tier1", "pcrd", "compact"), key=lambda k: st_mean[k])
+    model_bytes = 4.0 * counters[6] + counters[7]
+    mq_bytes = float(counters[7] + counters[3])
+    kernels = {
+        "dwt": ("dwt_batch_kernel (all levels)", dwt_bytes, st_mean["dwt"]),
+        "t1_model": ("t1_model_kernel", model_bytes, st_mean["t1_model"]),
+        "t1_mq": ("t1_mq_kernel", mq_bytes, st_mean["t1_mq"]),
+    }
+    def gbs(k):
+        _, b, ms = kernels[k]
+        return b / (ms / 1e3) / 1e9 if ms > 0 else None
+    dwt_gbs = gbs("dwt")
+    dominant = max(kernels, key=lambda k: kernels[k][2])
     traffic = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        traffic = prof.get(dominant)
+        traffic = prof.get(kernels[dominant][0].split(" ")[0])
     except Exception:
         pass
-    if dominant == "dwt":
-        roof = {"kernel": "dwt_level_kernel (all levels)", "bound": "hbm", "achieved": dwt_gbs,
-                "peak": hbm, "unit": "GB/s", "frac": dwt_gbs / hbm if dwt_gbs else None,
-                "traffic": traffic}
-    else:
-        roof = {"kernel": "t1_kernel", "bound": "hbm", "achieved": t1_gbs, "peak": hbm, "unit": "GB/s",
-                "frac": t1_gbs / hbm if t1_gbs else None, "traffic": traffic,
-                "note": "Tier-1 is issue/latency-bound (serial MQ per code-block); the HBM "
-                        "fraction shows how far it is from the bandwidth roof"}
+    roof = {"kernel": kernels[dominant][0], "bound": "hbm", "achieved": gbs(dominant), "peak": hbm,
+            "unit": "GB/s", "frac": gbs(dominant) / hbm if gbs(dominant) else None, "traffic": traffic,
+            "algorithmic_bytes_per_launch": kernels[dominant][1], "launch_ms": kernels[dominant][2]}
+    if dominant == "t1_mq":
+        roof["note"] = ("MQ coding is a serial chain per code-block, so a single page is bound by the "
+                        "heaviest block's chain latency, not by HBM; the fraction shows the distance "
+                        "to the bandwidth roof")
+        roof["mq_symbols_per_s"] = counters[7] / (st_mean["t1_mq"] / 1e3) if st_mean["t1_mq"] else None
     roof["peak_source"] = "measured" if "fallback" not in peaks else "fallback"
 
     line = {"metric": METRIC, "value": value, "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
@@ -455,6 +473,9 @@ def main():
             "roofline_dwt": {"bound": "hbm", "achieved": dwt_gbs, "peak": hbm, "unit": "GB/s",
                              "frac": dwt_gbs / hbm if dwt_gbs else None,
                              "algorithmic_bytes_per_launch_set": dwt_bytes},
+            "roofline_model": {"bound": "hbm", "achieved": gbs("t1_model"), "peak": hbm, "unit": "GB/s",
+                               "frac": gbs("t1_model") / hbm if gbs("t1_model") else None,
+                               "algorithmic_bytes_per_launch": model_bytes},
             "gpu_launches": int(counters[5]) * args.steps,
             "clocks": clocks.summary(),
             "output_bytes": int(np.mean(dev_sizes))}

@@ -109,8 +109,9 @@ int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, in
 /* Tuning knobs (the autotuner sets these):
  * JP2G_OPT_WAVE_BLOCKS        most code-blocks per device wave (default 160000);
  * JP2G_OPT_MQ_BLOCKS_PER_WARP code-blocks per warp in MQ coding, 1..32, or 0
- *                             for automatic (1 for small work lists, else 32);
- * JP2G_OPT_HOST_THREADS       host threads for staging and Tier-2 (0 = all). */
+ *                             for automatic (about 16 warps per SM);
+ * JP2G_OPT_HOST_THREADS       host threads for staging and Tier-2 (0 = all but
+ *                             two hardware threads). */
 enum {
   JP2G_OPT_WAVE_BLOCKS = 0,
   JP2G_OPT_MQ_BLOCKS_PER_WARP = 1,

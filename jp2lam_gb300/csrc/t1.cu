@@ -25,6 +25,8 @@
 //    and writing the byte stream to the block's payload slot.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstring>
 
 #include "jp2g_internal.h"
@@ -703,9 +705,14 @@ void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st) {
 }
 
 int mq_blocks_per_warp(const T1Args& a, int num_sms, int bpw) {
-  // Automatic: one block per warp while that keeps at most 48 warps per SM,
-  // 32 per warp beyond that.
-  if (bpw <= 0 || bpw > 32) bpw = a.nblocks <= (uint32_t)num_sms * 48u ? 1 : 32;
+  // Automatic: each warp is a latency-bound chain that issues about once
+  // every five cycles, so about 16 warps per SM keep its schedulers busy;
+  // pack as few blocks per warp as gives that many warps (lanes of a warp
+  // diverge, so fewer blocks per warp is faster while warps are plentiful).
+  if (bpw <= 0 || bpw > 32) {
+    const uint32_t target = (uint32_t)num_sms * 16u;
+    bpw = (int)std::min<uint32_t>(32u, std::max<uint32_t>(1u, (a.nblocks + target - 1) / target));
+  }
   return bpw;
 }
 
