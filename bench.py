@@ -410,13 +410,14 @@ def main():
     counters = eng.counters()
     tot_dev = sum(dev_t)
     tot_host = sum(host_t)
-    if dist:
-        t = torch.tensor([tot_dev, tot_host], device=f"cuda:{local}")
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        tot_dev, tot_host = t.tolist()
+    # replicas: every rank encodes its own pages; the slowest rank sets the
+    # job time (no collective on the data path)
+    from jp2lam_gb300 import replicas
+    tot_dev = replicas.max_over_ranks(tot_dev, device=f"cuda:{local}" if dist else None)
+    tot_host = replicas.max_over_ranks(tot_host, device=f"cuda:{local}" if dist else None)
     mpix = W * H / 1e6
-    value = world * args.steps * mpix / (tot_dev / 1e3)
-    e2e = world * args.steps * mpix / (tot_host / 1e3)
+    value = replicas.whole_job_rate(args.steps * mpix, world, tot_dev / 1e3)
+    e2e = replicas.whole_job_rate(args.steps * mpix, world, tot_host / 1e3)
 
     # stage breakdown (device-resident steps)
     keys = dev_st[0].keys()
