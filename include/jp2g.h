@@ -111,12 +111,19 @@ int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, in
  * JP2G_OPT_MQ_BLOCKS_PER_WARP code-blocks per warp in MQ coding, 1..32, or 0
  *                             for automatic (about 16 warps per SM);
  * JP2G_OPT_HOST_THREADS       host threads for staging and Tier-2 (0 = all but
- *                             two hardware threads). */
+ *                             two hardware threads);
+ * JP2G_OPT_MQ_WARPS_PER_SM    with one code-block per warp, the warps per SM
+ *                             that pull blocks heaviest first (0 = automatic:
+ *                             8 up to 16 blocks per SM, 12 up to 48; -1 = one
+ *                             warp per block, no pulling). With both MQ options
+ *                             automatic, work lists of up to 48 blocks per SM
+ *                             use pulling, larger ones packed warps. */
 enum {
   JP2G_OPT_WAVE_BLOCKS = 0,
   JP2G_OPT_MQ_BLOCKS_PER_WARP = 1,
   JP2G_OPT_HOST_THREADS = 2,
-  JP2G_NUM_OPTS = 3
+  JP2G_OPT_MQ_WARPS_PER_SM = 3,
+  JP2G_NUM_OPTS = 4
 };
 int jp2g_set_option(jp2g_ctx* ctx, int option, int64_t value);
 int jp2g_get_option(jp2g_ctx* ctx, int option, int64_t* value);

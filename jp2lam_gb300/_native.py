@@ -57,6 +57,7 @@ PENDING = 6
 OPT_WAVE_BLOCKS = 0
 OPT_MQ_BLOCKS_PER_WARP = 1
 OPT_HOST_THREADS = 2
+OPT_MQ_WARPS_PER_SM = 3
 
 
 class Request(ctypes.Structure):

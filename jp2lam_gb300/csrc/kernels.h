@@ -69,6 +69,9 @@ void launch_t1_items(const T1Args& a, cudaStream_t st);
 void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st);
 // bpw: code-blocks per warp, 1..32, or 0 for automatic.
 void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st);
+// One block per warp, blocks taken in a.mq_order from an atomic counter
+// (*next, zeroed here) by warps_per_sm warps on each SM.
+void launch_t1_mq_pull(const T1Args& a, int num_sms, int warps_per_sm, uint32_t* next, cudaStream_t st);
 // Code-blocks per warp that launch_t1_mq uses for `bpw` (0 = automatic).
 int mq_blocks_per_warp(const T1Args& a, int num_sms, int bpw);
 // Orders the blocks by their MQ symbol count, largest first (counting sort

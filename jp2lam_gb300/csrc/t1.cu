@@ -588,9 +588,8 @@ __device__ __forceinline__ void mq_chunk_part(Mq& m, uint2* ce, const uint2* T, 
 // flight to fill the GPU, 1 when a single page leaves it mostly idle and the
 // longest block's serial chain sets the time (lanes of a warp diverge on
 // every byte emitted, which lengthens each lane's chain).
-__global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw) {
-  __shared__ uint2 T[94];
-  __shared__ uint2 ce_all[kMqWarps][20 * 32];
+// The 94 state entries in the layout mq_step uses.
+__device__ __forceinline__ void load_mq_table(uint2* T) {
   for (int i = threadIdx.x; i < 94; i += blockDim.x) {
     // (qe | nmps << 16 | nlps << 24) -> the entry layout of mq_step
     const uint32_t v = c_tables.mq[i];
@@ -598,14 +597,11 @@ __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw)
     T[i] = make_uint2(qe | ((uint32_t)(__clz(qe) - 16) << 16) | ((uint32_t)(i & 1) << 20),
                       ((v >> 16) & 0xffu) | (((v >> 24) & 0xffu) << 8));
   }
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int wid = threadIdx.x >> 5;
-  if (lane >= bpw) return;
-  uint2* ce = &ce_all[wid][lane];  // context c at ce[32 * c]
-  const uint32_t slot = (blockIdx.x * kMqWarps + wid) * (uint32_t)bpw + (uint32_t)lane;
-  if (slot >= a.nblocks) return;
-  const uint32_t b = a.mq_order ? a.mq_order[slot] : slot;
+}
+
+// MQ-codes code-block b on the calling lane; ce is the lane's context
+// column (context c at ce[32 * c]).
+__device__ __forceinline__ void mq_code_block(const T1Args& a, uint32_t b, uint2* ce, const uint2* T) {
   BlockOut o = a.res[b];
   const int mbp = o.status ? 0 : o.mbp;
   if (mbp == 0) return;
@@ -673,6 +669,37 @@ __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw)
   atomicAdd(a.sym_count, (unsigned long long)nsym);
 }
 
+// Static mapping: warp w codes blocks order[w * bpw + lane], lanes < bpw.
+__global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw) {
+  __shared__ uint2 T[94];
+  __shared__ uint2 ce_all[kMqWarps][20 * 32];
+  load_mq_table(T);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  if (lane >= bpw) return;
+  const uint32_t slot = (blockIdx.x * kMqWarps + wid) * (uint32_t)bpw + (uint32_t)lane;
+  if (slot >= a.nblocks) return;
+  mq_code_block(a, a.mq_order ? a.mq_order[slot] : slot, &ce_all[wid][lane], T);
+}
+
+// Persistent form for one block per warp: a fixed number of warps per SM
+// take the next block of the order (heaviest first) until none is left, so
+// the longest chains start first and share their schedulers with few others.
+__global__ void __launch_bounds__(kMqWarps * 32) t1_mq_pull_kernel(T1Args a, uint32_t* next) {
+  __shared__ uint2 T[94];
+  __shared__ uint2 ce_all[kMqWarps][20 * 32];
+  load_mq_table(T);
+  __syncthreads();
+  if ((threadIdx.x & 31) != 0) return;
+  uint2* ce = &ce_all[threadIdx.x >> 5][0];
+  for (;;) {
+    const uint32_t slot = atomicAdd(next, 1u);
+    if (slot >= a.nblocks) return;
+    mq_code_block(a, a.mq_order[slot], ce, T);
+  }
+}
+
 }  // namespace
 
 bool upload_t1_tables(const uint8_t* zc, const uint8_t* sc, const uint8_t* spb,
@@ -721,6 +748,14 @@ void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st) {
   bpw = mq_blocks_per_warp(a, num_sms, bpw);
   const uint32_t per_cta = (uint32_t)bpw * kMqWarps;
   t1_mq_kernel<<<(a.nblocks + per_cta - 1) / per_cta, kMqWarps * 32, 0, st>>>(a, bpw);
+}
+
+void launch_t1_mq_pull(const T1Args& a, int num_sms, int warps_per_sm, uint32_t* next, cudaStream_t st) {
+  if (a.nblocks == 0) return;
+  cudaMemsetAsync(next, 0, sizeof(uint32_t), st);
+  const uint32_t ctas = std::min<uint32_t>((uint32_t)num_sms * (uint32_t)warps_per_sm / kMqWarps,
+                                           (a.nblocks + kMqWarps - 1) / kMqWarps);
+  t1_mq_pull_kernel<<<std::max<uint32_t>(ctas, 1u), kMqWarps * 32, 0, st>>>(a, next);
 }
 
 namespace {

@@ -173,3 +173,17 @@ def test_server_and_batch_encoder_api(eng):
     with pytest.raises(jl.InvalidInput):
         enc.encode_all([imgs[0], imgs[1], other])
     assert enc.encoded_count() == 2
+
+
+@pytest.mark.parametrize("wps", [-1, 1, 8, 64])
+def test_mq_pull_warps_do_not_change_output(eng, wps):
+    w, h = 600, 500
+    px = synth_page(w, h, 1, 91, photo_w=200, photo_h=150)
+    old = eng.get_option(_native.OPT_MQ_WARPS_PER_SM)
+    eng.set_option(_native.OPT_MQ_WARPS_PER_SM, -1)
+    ref = eng.encode(px, w, h, 1, 85, 1)
+    try:
+        eng.set_option(_native.OPT_MQ_WARPS_PER_SM, wps)
+        assert eng.encode(px, w, h, 1, 85, 1) == ref
+    finally:
+        eng.set_option(_native.OPT_MQ_WARPS_PER_SM, old)
