@@ -117,13 +117,20 @@ int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, in
  *                             8 up to 16 blocks per SM, 12 up to 48; -1 = one
  *                             warp per block, no pulling). With both MQ options
  *                             automatic, work lists of up to 48 blocks per SM
- *                             use pulling, larger ones packed warps. */
+ *                             use pulling, larger ones packed warps;
+ * JP2G_OPT_MQ_PIPES_PER_SM    when pulling: producer/consumer warp pairs per
+ *                             SM that split each block's MQ chain into its
+ *                             interval and code-register halves (0 =
+ *                             automatic: 8 pairs up to 16 blocks per SM,
+ *                             single-warp pulling above; -1 = single-warp
+ *                             pulling). */
 enum {
   JP2G_OPT_WAVE_BLOCKS = 0,
   JP2G_OPT_MQ_BLOCKS_PER_WARP = 1,
   JP2G_OPT_HOST_THREADS = 2,
   JP2G_OPT_MQ_WARPS_PER_SM = 3,
-  JP2G_NUM_OPTS = 4
+  JP2G_OPT_MQ_PIPES_PER_SM = 4,
+  JP2G_NUM_OPTS = 5
 };
 int jp2g_set_option(jp2g_ctx* ctx, int option, int64_t value);
 int jp2g_get_option(jp2g_ctx* ctx, int option, int64_t* value);

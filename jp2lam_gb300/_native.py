@@ -58,6 +58,7 @@ OPT_WAVE_BLOCKS = 0
 OPT_MQ_BLOCKS_PER_WARP = 1
 OPT_HOST_THREADS = 2
 OPT_MQ_WARPS_PER_SM = 3
+OPT_MQ_PIPES_PER_SM = 4
 
 
 class Request(ctypes.Structure):

@@ -669,6 +669,292 @@ __device__ __forceinline__ void mq_code_block(const T1Args& a, uint32_t b, uint2
   atomicAdd(a.sym_count, (unsigned long long)nsym);
 }
 
+// ------------------------------------------------- two-warp MQ pipeline --
+// For one code-block at a time, the MQ coder splits into two chains: the
+// interval and context-state chain (A register, probability states) and the
+// code register chain (C register, byte output). The first never depends on
+// the second, so a producer warp runs it over 16-symbol chunks, handing each
+// symbol's (qe added to C | shift << 16) to a consumer warp that runs the C
+// chain, writes the bytes and records numbytes() at every pass end, one
+// chunk behind. All 32 lanes of each warp run the same chain (so the
+// barriers and the byte stores need no lane masks). Each pair of warps
+// pulls blocks, heaviest first, from an atomic counter.
+constexpr int kPipes = 4;  // pipelines (warp pairs) per CTA
+constexpr uint32_t kPipeEnd = 0xffffffffu;
+
+struct PipeChunk {
+  uint32_t block;  // code-block, or kPipeEnd
+  uint16_t item;   // item (bit-plane) index within the block
+  uint16_t lo;     // first symbol of the chunk within the item
+  uint32_t count;  // symbols in the chunk, 0..16
+  uint32_t flags;  // 1: first chunk of the block, 2: last of its item, 4: last of the block
+  uint32_t a_end;  // A after the block's last symbol (flags & 4)
+  uint32_t op[16];
+};
+
+__device__ __forceinline__ void pipe_bar(int id) {
+  asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory");
+}
+
+// State entry with its successors: x = qe | leading zeros of qe << 16 |
+// MPS << 20, y and z the x of the states after an MPS and an LPS
+// renormalisation, w their indices (MPS | LPS << 8).
+__device__ __forceinline__ void load_fat_table(uint4* F) {
+  for (int i = threadIdx.x; i < 94; i += blockDim.x) {
+    auto xs = [](int k) {
+      const uint32_t v = c_tables.mq[k], qe = v & 0xffffu;
+      return qe | ((uint32_t)(__clz(qe) - 16) << 16) | ((uint32_t)(k & 1) << 20);
+    };
+    const uint32_t v = c_tables.mq[i], nm = (v >> 16) & 0xffu, nl = (v >> 24) & 0xffu;
+    F[i] = make_uint4(xs(i), xs((int)nm), xs((int)nl), nm | (nl << 8));
+  }
+}
+
+// Interval/state step of one symbol whose context state index is ci[cx];
+// returns the symbol's C operation (see mq_step for the folded decisions).
+__device__ __forceinline__ uint32_t phase_a_one(uint32_t& A, uint32_t* ci, const uint4* F, uint32_t sym) {
+  const uint32_t cx = sym >> 1, cur = ci[cx];
+  const uint4 f = F[cur];
+  const uint32_t qe = f.x & 0xffffu;
+  const uint32_t lps = ((f.x >> 20) ^ sym) & 1u;
+  const uint32_t a = A - qe;
+  const bool take_a = (a < qe) == (lps != 0);
+  const uint32_t n = take_a ? ((a < 0x4000u ? 1u : 0u) + (a < 0x8000u ? 1u : 0u)) : ((f.x >> 16) & 15u);
+  A = (take_a ? a : qe) << n;
+  ci[cx] = n ? (lps ? (f.w >> 8) : (f.w & 0xffu)) : cur;
+  return (take_a ? qe : 0u) | (n << 16);
+}
+
+// The same over a full chunk: the next state's qe comes from the current
+// entry (no load on the chain), context indices are read two symbols ahead
+// and forwarded when a context repeats.
+__device__ __forceinline__ void phase_a_chunk(uint32_t& A, uint32_t* ci, const uint4* F, const uint4 q,
+                                              uint32_t (&op)[16]) {
+  uint32_t sy[16];
+  #pragma unroll
+  for (int i = 0; i < 16; ++i) sy[i] = chunk_sym(q, i);
+  uint32_t cur = ci[sy[0] >> 1];
+  uint4 f = F[cur];
+  uint32_t idx_next = ci[sy[1] >> 1];
+  uint4 fl_next = F[idx_next];
+  #pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const uint32_t cx = sy[i] >> 1;
+    uint32_t raw2 = 0;
+    if (i + 2 < 16) raw2 = ci[sy[i + 2] >> 1];  // before this symbol's update
+    const uint32_t qe = f.x & 0xffffu;
+    const uint32_t lps = ((f.x >> 20) ^ sy[i]) & 1u;
+    const uint32_t a = A - qe;
+    const bool take_a = (a < qe) == (lps != 0);
+    const uint32_t n = take_a ? ((a < 0x4000u ? 1u : 0u) + (a < 0x8000u ? 1u : 0u)) : ((f.x >> 16) & 15u);
+    A = (take_a ? a : qe) << n;
+    op[i] = (take_a ? qe : 0u) | (n << 16);
+    const uint32_t newidx = n ? (lps ? (f.w >> 8) : (f.w & 0xffu)) : cur;
+    const uint32_t newx = n ? (lps ? f.z : f.y) : f.x;
+    ci[cx] = newidx;
+    if (i + 1 < 16) {
+      const uint4 L = F[newidx];
+      const uint32_t cxn = sy[i + 1] >> 1;
+      if (cxn == cx) {
+        f = make_uint4(newx, L.y, L.z, L.w);
+        cur = newidx;
+      } else {
+        f = fl_next;
+        cur = idx_next;
+      }
+      if (i + 2 < 16) {
+        idx_next = (sy[i + 2] >> 1) == cx ? newidx : raw2;
+        fl_next = F[idx_next];
+      }
+    }
+  }
+}
+
+// Code-register step of one symbol's operation (byte output as needed).
+__device__ __forceinline__ void phase_c_one(Mq& m, uint32_t op) {
+  m.c += op & 0xffffu;
+  uint32_t n = op >> 16;
+  if (n >= m.ct) {
+    do {
+      m.c <<= m.ct;
+      n -= m.ct;
+      mq_byteout(m);
+    } while (n >= m.ct);
+  }
+  m.c <<= n;
+  m.ct -= n;
+}
+
+__global__ void __launch_bounds__(kPipes * 64) t1_mq_pipe_kernel(T1Args a, uint32_t* next) {
+  __shared__ uint4 F[94];
+  __shared__ PipeChunk slots[kPipes][2];
+  __shared__ uint32_t ci_all[kPipes][20];
+  load_fat_table(F);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pipe = warp >> 1;
+  const int bar = 1 + pipe;
+  PipeChunk* slot = slots[pipe];
+  if ((warp & 1) == 0) {
+    // ---- producer: interval and state chain ----
+    uint32_t* ci = ci_all[pipe];
+    uint32_t b = kPipeEnd, base = 0, A = 0x8000u;
+    int mbp = 0, j = 0, lo = 0, total = 0;
+    const uint4* src = nullptr;
+    uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0, c2 = c0;
+    auto start_item = [&]() {
+      const ItemRec r = a.item_rec[base + j];
+      total = (int)(r.n_sp + r.n_mr + r.n_cl);
+      lo = 0;
+      src = reinterpret_cast<const uint4*>(a.sym + (size_t)(base + j) * a.sym_slot);
+      c0 = src[0];
+      c1 = src[1];
+      c2 = src[2];  // the slot and the buffer are padded for these reads
+    };
+    for (uint32_t k = 0;; ++k) {
+      PipeChunk& s = slot[k & 1];
+      uint32_t flags = 0;
+      while (b == kPipeEnd) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(next, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= a.nblocks) break;
+        const uint32_t cand = a.mq_order[t];
+        const BlockOut o = a.res[cand];
+        const int m_ = o.status ? 0 : o.mbp;
+        if (m_ == 0) continue;
+        b = cand;
+        mbp = m_;
+        j = 0;
+        base = a.plane_base[b];
+        A = 0x8000u;
+        // contexts: state 0 except UNI 46, AGG 3, ZC 4 (src/mq/mod.rs:195-200)
+        if (lane < 19) ci[lane] = lane == kCtxUNI ? 92u : (lane == kCtxAGG ? 6u : (lane == 0 ? 8u : 0u));
+        __syncwarp();
+        flags = 1;
+        start_item();
+      }
+      if (b == kPipeEnd) {
+        if (lane == 0) s.block = kPipeEnd;
+        __syncwarp();
+        pipe_bar(bar);
+        break;
+      }
+      const int cnt = min(16, total - lo);
+      if (cnt == 16) {
+        const uint4 q = c0;
+        c0 = c1;
+        c1 = c2;
+        c2 = src[(lo >> 4) + 3];  // 48 bytes ahead: inside the slot or the buffer's pad
+        uint32_t op[16];
+        phase_a_chunk(A, ci, F, q, op);
+        if (lane == 0) {
+          #pragma unroll
+          for (int i = 0; i < 16; ++i) s.op[i] = op[i];
+        }
+      } else {
+        const uint4 q = c0;
+        for (int i = 0; i < cnt; ++i) {
+          const uint32_t o = phase_a_one(A, ci, F, chunk_sym(q, i));
+          if (lane == 0) s.op[i] = o;
+        }
+      }
+      if (lane == 0) {
+        s.block = b;
+        s.item = (uint16_t)j;
+        s.lo = (uint16_t)lo;
+        s.count = (uint32_t)cnt;
+      }
+      lo += cnt;
+      if (lo >= total) {
+        flags |= 2;
+        if (++j == mbp) {
+          flags |= 4;
+          if (lane == 0) s.a_end = A;
+          b = kPipeEnd;
+        } else {
+          start_item();
+        }
+      }
+      if (lane == 0) s.flags = flags;
+      __syncwarp();
+      pipe_bar(bar);
+    }
+  } else {
+    // ---- consumer: code register chain, bytes and pass records ----
+    Mq m{0x8000u, 0u, 12u, 0, 0u, nullptr, 0, 0};
+    BlockOut o{};
+    PassRec* pr = nullptr;
+    ItemRec r{};
+    uint32_t base = 0, nsym = 0;
+    int pi = 0, npass = 1, kp = 0;
+    int end[3] = {0, 0, 0};
+    auto snapshot = [&](int k, int item) {  // numbytes() after pass k
+      const uint8_t bp = (uint8_t)r.bitplane;
+      if (npass == 1 || k == 2)
+        pr[pi] = PassRec{(uint32_t)m.pos, r.ns_cl, item == 0 ? 0u : r.sig_before + r.ns_sp, 2, bp, 0};
+      else if (k == 0)
+        pr[pi] = PassRec{(uint32_t)m.pos, r.ns_sp, r.sig_before, 0, bp, 0};
+      else
+        pr[pi] = PassRec{(uint32_t)m.pos, 0u, r.sig_before, 1, bp, 0};
+      ++pi;
+    };
+    for (uint32_t k = 0;; ++k) {
+      pipe_bar(bar);
+      const PipeChunk& s = slot[k & 1];
+      const uint32_t blk = s.block;
+      if (blk == kPipeEnd) break;
+      const uint32_t flags = s.flags;
+      const int item = s.item, lo = s.lo, cnt = (int)s.count;
+      if (flags & 1) {
+        const BlockDesc d = a.blocks[blk];
+        o = a.res[blk];
+        m = Mq{0x8000u, 0u, 12u, 0, 0u, a.out + d.out_off, (int)d.out_cap, 0};
+        pr = a.passes + d.pass_off;
+        pi = 0;
+        nsym = 0;
+        base = a.plane_base[blk];
+      }
+      if (lo == 0) {
+        r = a.item_rec[base + item];
+        const int total = (int)(r.n_sp + r.n_mr + r.n_cl);
+        npass = item == 0 ? 1 : 3;
+        end[0] = item == 0 ? total : (int)r.n_sp;
+        end[1] = (int)(r.n_sp + r.n_mr);
+        end[2] = total;
+        nsym += (uint32_t)total;
+        kp = 0;
+        while (kp < npass - 1 && end[kp] == 0) snapshot(kp++, item);
+      }
+      const int hi = lo + cnt;
+      if (cnt == 16 && (kp == npass - 1 || end[kp] >= hi)) {
+        uint32_t op[16];
+        #pragma unroll
+        for (int i = 0; i < 16; ++i) op[i] = s.op[i];
+        #pragma unroll
+        for (int i = 0; i < 16; ++i) phase_c_one(m, op[i]);
+      } else {
+        for (int i = 0; i < cnt; ++i) {
+          phase_c_one(m, s.op[i]);
+          while (kp < npass - 1 && end[kp] == lo + i + 1) snapshot(kp++, item);
+        }
+      }
+      while (kp < npass - 1 && end[kp] == hi) snapshot(kp++, item);
+      if (flags & 2) snapshot(npass == 1 ? 0 : 2, item);
+      if (flags & 4) {
+        m.a = s.a_end;
+        mq_flush(m);
+        o.payload_len = (uint32_t)(m.last == 0xffu ? m.pos - 1 : m.pos);  // take_bytes
+        o.status = m.ovf ? 1 : 0;
+        if (lane == 0) {
+          a.res[blk] = o;
+          atomicAdd(a.sym_count, (unsigned long long)nsym);
+        }
+      }
+    }
+  }
+}
+
 // Static mapping: warp w codes blocks order[w * bpw + lane], lanes < bpw.
 __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_kernel(T1Args a, int bpw) {
   __shared__ uint2 T[94];
@@ -748,6 +1034,14 @@ void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st) {
   bpw = mq_blocks_per_warp(a, num_sms, bpw);
   const uint32_t per_cta = (uint32_t)bpw * kMqWarps;
   t1_mq_kernel<<<(a.nblocks + per_cta - 1) / per_cta, kMqWarps * 32, 0, st>>>(a, bpw);
+}
+
+void launch_t1_mq_pipe(const T1Args& a, int num_sms, int pipes_per_sm, uint32_t* next, cudaStream_t st) {
+  if (a.nblocks == 0) return;
+  cudaMemsetAsync(next, 0, sizeof(uint32_t), st);
+  const uint32_t ctas = std::min<uint32_t>((uint32_t)num_sms * (uint32_t)pipes_per_sm / kPipes,
+                                           (a.nblocks + kPipes - 1) / kPipes);
+  t1_mq_pipe_kernel<<<std::max<uint32_t>(ctas, 1u), kPipes * 64, 0, st>>>(a, next);
 }
 
 void launch_t1_mq_pull(const T1Args& a, int num_sms, int warps_per_sm, uint32_t* next, cudaStream_t st) {

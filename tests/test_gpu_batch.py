@@ -175,15 +175,17 @@ def test_server_and_batch_encoder_api(eng):
     assert enc.encoded_count() == 2
 
 
-@pytest.mark.parametrize("wps", [-1, 1, 8, 64])
-def test_mq_pull_warps_do_not_change_output(eng, wps):
+@pytest.mark.parametrize("wps,pipes", [(-1, 0), (1, -1), (8, -1), (64, -1), (0, 1), (0, 4), (0, 32)])
+@pytest.mark.parametrize("q", [85, 100, 20])
+def test_mq_schedules_do_not_change_output(eng, orc, wps, pipes, q):
+    # static warps, single-warp pulling and producer/consumer pipelines
     w, h = 600, 500
     px = synth_page(w, h, 1, 91, photo_w=200, photo_h=150)
-    old = eng.get_option(_native.OPT_MQ_WARPS_PER_SM)
-    eng.set_option(_native.OPT_MQ_WARPS_PER_SM, -1)
-    ref = eng.encode(px, w, h, 1, 85, 1)
+    old = eng.get_option(_native.OPT_MQ_WARPS_PER_SM), eng.get_option(_native.OPT_MQ_PIPES_PER_SM)
     try:
         eng.set_option(_native.OPT_MQ_WARPS_PER_SM, wps)
-        assert eng.encode(px, w, h, 1, 85, 1) == ref
+        eng.set_option(_native.OPT_MQ_PIPES_PER_SM, pipes)
+        assert eng.encode(px, w, h, 1, q, 1) == orc.encode(px, w, h, 1, q, 1)
     finally:
-        eng.set_option(_native.OPT_MQ_WARPS_PER_SM, old)
+        eng.set_option(_native.OPT_MQ_WARPS_PER_SM, old[0])
+        eng.set_option(_native.OPT_MQ_PIPES_PER_SM, old[1])
