@@ -245,8 +245,8 @@ def bench_uneven(eng, stream, torch, dev, args):
     mpix = sum(p["w"] * p["h"] for p in pages) / 1e6
     bufs, dpages = _to_device(pages, torch, dev)
     torch.cuda.synchronize()
-    dev_t = _time_calls(lambda: eng.encode_batch(dpages), 2, 1, stream, torch)
-    host_t = _time_calls(lambda: eng.encode_batch(pages), 2, 1, stream, torch)
+    dev_t = _time_calls(lambda: eng.encode_batch(dpages), 3, 2, stream, torch)
+    host_t = _time_calls(lambda: eng.encode_batch(pages), 3, 2, stream, torch)
     plain_t = _time_calls(lambda: [eng.encode_device(p["px"], p["w"], p["h"], p["ncomp"], p["quality"],
                                                      p["fmt"]) for p in dpages], 1, 1, stream, torch)
     del bufs

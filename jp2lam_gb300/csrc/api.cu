@@ -94,7 +94,7 @@ struct jp2g_ctx {
       hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym, stats, dwtargs,
       dwtbases, mqorder, mqscratch;
   // pinned host staging
-  HostBuf hpx, hkeep, hoffsets, hbody, hres, hcount;
+  HostBuf hpx, hpx2, hkeep, hoffsets, hbody, hres, hcount;
   bool timing = false;
   cudaEvent_t ev[kNumEvents] = {};
   float stage_ms[kNumStages + 3] = {};
@@ -418,13 +418,68 @@ struct WaveDebug {
   std::vector<BlockOut>* res = nullptr;
 };
 
+// Pixels of a wave's host-memory pages, staged in pinned memory.
+struct Prestaged {
+  HostBuf* buf;
+  size_t total;
+};
+constexpr size_t kStageFailed = ~size_t(0);
+
+// Copies the host pixels of the valid pages among jobs into `buf` (pinned,
+// grown as needed), interleaving planar RGB (Image::from_rgb_bytes takes
+// RGBRGB), and sets each page's px_off. The copy is split into 2 MiB tasks
+// over the host threads. Returns the bytes staged, or kStageFailed.
+size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
+  size_t total = 0;
+  std::vector<PageJob*> host;
+  for (size_t i = 0; i < n; ++i) {
+    PageJob* j = jobs[i];
+    PagePlan p;
+    Failure f{};
+    if (!j->host_px || !build_plan(j->w, j->h, (int)j->ncomp, j->quality, j->format, &p, &f)) continue;
+    j->px_off = total;
+    total += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
+    host.push_back(j);
+  }
+  if (total == 0) return 0;
+  if (!reserve_host(c, buf, total)) return kStageFailed;
+  uint8_t* staging = reinterpret_cast<uint8_t*>(buf.p);
+  struct CopyTask {
+    const PageJob* j;
+    size_t p0, p1;  // pixel range
+  };
+  std::vector<CopyTask> tasks;
+  for (const PageJob* j : host) {
+    const size_t np = (size_t)j->w * j->h, step = std::max<size_t>((2u << 20) / j->ncomp, 1);
+    for (size_t p0 = 0; p0 < np; p0 += step) tasks.push_back({j, p0, std::min(np, p0 + step)});
+  }
+  parallel_for(tasks.size(), total > (4u << 20) ? host_threads(c) : 1, [&](size_t k) {
+    const CopyTask& t = tasks[k];
+    const PageJob* j = t.j;
+    uint8_t* dst = staging + j->px_off;
+    const size_t np = (size_t)j->w * j->h;
+    if (j->ncomp == 3 && !j->interleaved) {
+      for (size_t i = t.p0; i < t.p1; ++i) {
+        dst[3 * i + 0] = j->host_px[i];
+        dst[3 * i + 1] = j->host_px[np + i];
+        dst[3 * i + 2] = j->host_px[2 * np + i];
+      }
+    } else {
+      std::memcpy(dst + t.p0 * j->ncomp, j->host_px + t.p0 * j->ncomp, (t.p1 - t.p0) * j->ncomp);
+    }
+  });
+  return total;
+}
+
 // Device phase of a wave of pages: plans and validation, inputs,
 // colour+DWT+quantisation per page, then Tier-1, PCRD and compaction over
 // the wave's flat code-block list (all pages' blocks, page after page), and
 // the read-back of each page's retained blocks and bytes into its job. A page
 // that fails validation or overflows a block slot is marked and the rest
-// carry on; a CUDA failure fails the wave (return code).
-int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
+// carry on; a CUDA failure fails the wave (return code). `pre`: the wave's
+// host pixels already staged by stage_pixels (else they are staged here).
+int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
+             const Prestaged* pre = nullptr) {
   std::memset(c->counters, 0, sizeof c->counters);
   std::vector<PageJob*> live;
   int cbw = 0;
@@ -460,16 +515,11 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
   std::vector<BandParam> bands;
   std::vector<CompParam> comps;
   uint64_t nb64 = 0;
-  size_t hpx_total = 0;
   for (PageJob* j : live) {
     j->block_base = (uint32_t)nb64;
     build_tables(j->plan, j->block_base, (uint32_t)bands.size(), (uint32_t)comps.size(), cap, pcap,
                  &blocks, &bands, &comps);
     nb64 += j->plan.nblocks;
-    if (j->host_px) {
-      j->px_off = hpx_total;
-      hpx_total += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
-    }
   }
   if (nb64 * cap > 0xffffffffull)
     return set_err(c, kUnsupportedFeature,
@@ -499,30 +549,19 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg) {
 
   record(c, 0);
   // ---- inputs ----
+  size_t hpx_total = 0;
+  const uint8_t* staging = nullptr;
+  if (pre) {
+    hpx_total = pre->total;
+    staging = reinterpret_cast<const uint8_t*>(pre->buf->p);
+  } else {
+    hpx_total = stage_pixels(c, live.data(), live.size(), c->hpx);
+    if (hpx_total == kStageFailed) return kEncodeFailed;
+    staging = reinterpret_cast<const uint8_t*>(c->hpx.p);
+  }
   if (hpx_total > 0) {
-    if (!reserve(c, c->px, hpx_total) || !reserve_host(c, c->hpx, hpx_total)) return kEncodeFailed;
-    uint8_t* staging = reinterpret_cast<uint8_t*>(c->hpx.p);
-    std::vector<PageJob*> host_jobs;
-    for (PageJob* j : live)
-      if (j->host_px) host_jobs.push_back(j);
-    // Pixels go to pinned staging (interleaving planar RGB, which
-    // Image::from_rgb_bytes takes as RGBRGB) and on to the device.
-    parallel_for(host_jobs.size(), hpx_total > (64u << 20) ? host_threads(c) : 1, [&](size_t k) {
-      const PageJob* j = host_jobs[k];
-      uint8_t* dst = staging + j->px_off;
-      const size_t n = (size_t)j->w * j->h;
-      if (j->ncomp == 3 && !j->interleaved) {
-        for (size_t i = 0; i < n; ++i) {
-          dst[3 * i + 0] = j->host_px[i];
-          dst[3 * i + 1] = j->host_px[n + i];
-          dst[3 * i + 2] = j->host_px[2 * n + i];
-        }
-      } else {
-        std::memcpy(dst, j->host_px, n * j->ncomp);
-      }
-    });
-    if (!cuda_ok(c, cudaMemcpyAsync(c->px.p, staging, hpx_total, cudaMemcpyHostToDevice, c->stream),
-                 "H2D"))
+    if (!reserve(c, c->px, hpx_total) ||
+        !cuda_ok(c, cudaMemcpyAsync(c->px.p, staging, hpx_total, cudaMemcpyHostToDevice, c->stream), "H2D"))
       return kEncodeFailed;
   }
   if (!cuda_ok(c, cudaMemcpyAsync(c->blocks.p, blocks.data(), nb * sizeof(BlockDesc),
@@ -842,7 +881,7 @@ void jp2g_destroy(jp2g_ctx* c) {
                     &c->mqscratch};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
-  HostBuf* hb[] = {&c->hpx, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres, &c->hcount};
+  HostBuf* hb[] = {&c->hpx, &c->hpx2, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres, &c->hcount};
   for (HostBuf* b : hb)
     if (b->p) cudaFreeHost(b->p);
   for (auto& ev : c->ev)
@@ -931,8 +970,30 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
   uint64_t counters[8] = {};
   std::memset(c->stage_ms, 0, sizeof c->stage_ms);
   const auto t0 = std::chrono::steady_clock::now();
-  for (auto& wave : form_waves(c, ptrs)) {
-    rc = run_wave(c, wave.data(), wave.size(), nullptr);
+  // Host pixels of wave k+1 are staged (on a helper thread, into the other
+  // pinned buffer) while wave k is on the device.
+  auto waves = form_waves(c, ptrs);
+  HostBuf* bufs[2] = {&c->hpx, &c->hpx2};
+  size_t staged = stage_pixels(c, waves.empty() ? nullptr : waves[0].data(),
+                               waves.empty() ? 0 : waves[0].size(), *bufs[0]);
+  for (size_t w = 0; w < waves.size(); ++w) {
+    auto& wave = waves[w];
+    if (staged == kStageFailed) {
+      rc = JP2G_ENCODE_FAILED;
+      break;
+    }
+    size_t next_staged = 0;
+    std::thread stager;
+    if (w + 1 < waves.size()) {
+      stager = std::thread([&, w] {
+        cudaSetDevice(c->device);
+        next_staged = stage_pixels(c, waves[w + 1].data(), waves[w + 1].size(), *bufs[(w + 1) & 1]);
+      });
+    }
+    const Prestaged pre{bufs[w & 1], staged};
+    rc = run_wave(c, wave.data(), wave.size(), nullptr, &pre);
+    if (stager.joinable()) stager.join();
+    staged = next_staged;
     for (int k = 0; k < 8; ++k) counters[k] += c->counters[k];
     if (rc != JP2G_OK) break;
     add_wave_stage_times(c);
