@@ -123,14 +123,18 @@ int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, in
  *                             interval and code-register halves (0 =
  *                             automatic: 8 pairs up to 16 blocks per SM,
  *                             single-warp pulling above; -1 = single-warp
- *                             pulling). */
+ *                             pulling);
+ * JP2G_OPT_MQ_HEAVY           with pipelines: how many of the heaviest blocks
+ *                             they take, the rest being coded 32 to a warp
+ *                             (0 = all blocks). */
 enum {
   JP2G_OPT_WAVE_BLOCKS = 0,
   JP2G_OPT_MQ_BLOCKS_PER_WARP = 1,
   JP2G_OPT_HOST_THREADS = 2,
   JP2G_OPT_MQ_WARPS_PER_SM = 3,
   JP2G_OPT_MQ_PIPES_PER_SM = 4,
-  JP2G_NUM_OPTS = 5
+  JP2G_OPT_MQ_HEAVY = 5,
+  JP2G_NUM_OPTS = 6
 };
 int jp2g_set_option(jp2g_ctx* ctx, int option, int64_t value);
 int jp2g_get_option(jp2g_ctx* ctx, int option, int64_t* value);

@@ -59,6 +59,7 @@ OPT_MQ_BLOCKS_PER_WARP = 1
 OPT_HOST_THREADS = 2
 OPT_MQ_WARPS_PER_SM = 3
 OPT_MQ_PIPES_PER_SM = 4
+OPT_MQ_HEAVY = 5
 
 
 class Request(ctypes.Structure):

@@ -99,7 +99,7 @@ struct jp2g_ctx {
   cudaEvent_t ev[kNumEvents] = {};
   float stage_ms[kNumStages + 3] = {};
   uint64_t counters[8] = {};
-  int64_t opt[JP2G_NUM_OPTS] = {160000, 0, 0, 0, 0};
+  int64_t opt[JP2G_NUM_OPTS] = {160000, 0, 0, 0, 0, 0};
   // submit/poll: a worker thread forms waves from the queue and runs their
   // device phase; a finisher thread runs Tier-2 of finished waves, so the
   // next wave's device work overlaps the previous wave's host work.
@@ -642,8 +642,8 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
   const int64_t pipes_opt = c->opt[JP2G_OPT_MQ_PIPES_PER_SM];
   const bool use_pipe = use_pull && (pipes_opt > 0 || (pipes_opt == 0 && nb <= sms * 16u));
   if (use_pipe)
-    launch_t1_mq_pipe(ta, c->num_sms, pipes_opt > 0 ? (int)pipes_opt : 8, dptr<uint32_t>(c->stats) + 2,
-                      c->stream);
+    launch_t1_mq_pipe(ta, c->num_sms, pipes_opt > 0 ? (int)pipes_opt : 8, (uint32_t)c->opt[JP2G_OPT_MQ_HEAVY],
+                      dptr<uint32_t>(c->stats) + 2, c->stream);
   else if (use_pull)
     launch_t1_mq_pull(ta, c->num_sms, pull, dptr<uint32_t>(c->stats) + 2, c->stream);
   else
@@ -1171,6 +1171,9 @@ int jp2g_set_option(jp2g_ctx* c, int option, int64_t value) {
       break;
     case JP2G_OPT_MQ_PIPES_PER_SM:
       if (value < -1 || value > 32) return set_err(c, JP2G_INVALID_INPUT, "mq_pipes_per_sm must be -1..32");
+      break;
+    case JP2G_OPT_MQ_HEAVY:
+      if (value < 0 || value > 0xffffffffll) return set_err(c, JP2G_INVALID_INPUT, "mq_heavy must be >= 0");
       break;
     default:
       return set_err(c, JP2G_INVALID_INPUT, "unknown option " + std::to_string(option));

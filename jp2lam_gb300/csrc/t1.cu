@@ -785,10 +785,24 @@ __device__ __forceinline__ void phase_c_one(Mq& m, uint32_t op) {
   m.ct -= n;
 }
 
-__global__ void __launch_bounds__(kPipes * 64) t1_mq_pipe_kernel(T1Args a, uint32_t* next) {
+// CTAs below pipe_ctas are pipelines that pull the `heavy` heaviest blocks;
+// the CTAs above code the remaining (lighter) blocks 32 to a warp, one per
+// lane, which costs the schedulers far fewer issue slots per symbol.
+__global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, uint32_t* next, uint32_t pipe_ctas,
+                                                                uint32_t heavy) {
   __shared__ uint4 F[94];
   __shared__ PipeChunk slots[kPipes][2];
   __shared__ uint32_t ci_all[kPipes][20];
+  if (blockIdx.x >= pipe_ctas) {
+    __shared__ uint2 T[94];
+    __shared__ uint2 ce_all[kPipes * 2][20 * 32];
+    load_mq_table(T);
+    __syncthreads();
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const uint32_t slot = heavy + ((blockIdx.x - pipe_ctas) * (kPipes * 2) + (uint32_t)w) * 32u + (uint32_t)l;
+    if (slot < a.nblocks) mq_code_block(a, a.mq_order[slot], &ce_all[w][l], T);
+    return;
+  }
   load_fat_table(F);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -818,7 +832,7 @@ __global__ void __launch_bounds__(kPipes * 64) t1_mq_pipe_kernel(T1Args a, uint3
         uint32_t t = 0;
         if (lane == 0) t = atomicAdd(next, 1u);
         t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= a.nblocks) break;
+        if (t >= heavy) break;
         const uint32_t cand = a.mq_order[t];
         const BlockOut o = a.res[cand];
         const int m_ = o.status ? 0 : o.mbp;
@@ -1036,12 +1050,16 @@ void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st) {
   t1_mq_kernel<<<(a.nblocks + per_cta - 1) / per_cta, kMqWarps * 32, 0, st>>>(a, bpw);
 }
 
-void launch_t1_mq_pipe(const T1Args& a, int num_sms, int pipes_per_sm, uint32_t* next, cudaStream_t st) {
+void launch_t1_mq_pipe(const T1Args& a, int num_sms, int pipes_per_sm, uint32_t heavy, uint32_t* next,
+                       cudaStream_t st) {
   if (a.nblocks == 0) return;
   cudaMemsetAsync(next, 0, sizeof(uint32_t), st);
-  const uint32_t ctas = std::min<uint32_t>((uint32_t)num_sms * (uint32_t)pipes_per_sm / kPipes,
-                                           (a.nblocks + kPipes - 1) / kPipes);
-  t1_mq_pipe_kernel<<<std::max<uint32_t>(ctas, 1u), kPipes * 64, 0, st>>>(a, next);
+  heavy = heavy == 0 ? a.nblocks : std::min(heavy, a.nblocks);
+  const uint32_t pipe_ctas = std::max<uint32_t>(
+      1u, std::min<uint32_t>((uint32_t)num_sms * (uint32_t)pipes_per_sm / kPipes, (heavy + kPipes - 1) / kPipes));
+  const uint32_t per_cta = kPipes * 2 * 32;
+  const uint32_t packed_ctas = (a.nblocks - heavy + per_cta - 1) / per_cta;
+  t1_mq_pipe_kernel<<<pipe_ctas + packed_ctas, kPipes * 64, 0, st>>>(a, next, pipe_ctas, heavy);
 }
 
 void launch_t1_mq_pull(const T1Args& a, int num_sms, int warps_per_sm, uint32_t* next, cudaStream_t st) {
