@@ -109,15 +109,14 @@ int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, in
 /* Tuning knobs (the autotuner sets these):
  * JP2G_OPT_WAVE_BLOCKS        most code-blocks per device wave (default 160000);
  * JP2G_OPT_MQ_BLOCKS_PER_WARP code-blocks per warp in MQ coding, 1..32, or 0
- *                             for automatic (about 16 warps per SM);
+ *                             for automatic (1 up to 16 blocks per SM, else
+ *                             2..32 for about 24 warps per SM);
  * JP2G_OPT_HOST_THREADS       host threads for staging and Tier-2 (0 = all but
  *                             two hardware threads);
  * JP2G_OPT_MQ_WARPS_PER_SM    with one code-block per warp, the warps per SM
  *                             that pull blocks heaviest first (0 = automatic:
- *                             8 up to 16 blocks per SM, 12 up to 48; -1 = one
- *                             warp per block, no pulling). With both MQ options
- *                             automatic, work lists of up to 48 blocks per SM
- *                             use pulling, larger ones packed warps;
+ *                             8 up to 16 blocks per SM, else 12; -1 = one warp
+ *                             per block, no pulling);
  * JP2G_OPT_MQ_PIPES_PER_SM    when pulling: producer/consumer warp pairs per
  *                             SM that split each block's MQ chain into its
  *                             interval and code-register halves (0 =

@@ -618,14 +618,13 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
   // warp's lanes carry similar symbol counts; with one block per warp by a
   // fixed number of warps per SM that pull blocks in that order, so the
   // longest chains start first and share their schedulers with few others.
-  // Automatic choice (measured on 2550x3300 and 3400x4400 pages): up to 48
-  // blocks per SM, one block per warp pulled by 8 (up to 16 blocks per SM)
-  // or 12 warps per SM; beyond that, blocks packed into warps.
+  // Automatic choice (measured on 1275x1650 to 3400x4400 pages): up to 16
+  // blocks per SM, producer/consumer pipelines pulling one block each;
+  // beyond that, 2..32 blocks packed per warp.
   const int64_t bpw_opt = c->opt[JP2G_OPT_MQ_BLOCKS_PER_WARP];
   const int64_t wps_opt = c->opt[JP2G_OPT_MQ_WARPS_PER_SM];
   const uint32_t sms = (uint32_t)c->num_sms;
-  const bool few = nb <= sms * 48u;
-  const int bpw = bpw_opt == 0 && few && wps_opt >= 0 ? 1 : mq_blocks_per_warp(ta, c->num_sms, (int)bpw_opt);
+  const int bpw = mq_blocks_per_warp(ta, c->num_sms, (int)bpw_opt);
   const bool use_pull = bpw == 1 && wps_opt >= 0;
   const int pull = wps_opt > 0 ? (int)wps_opt : (nb <= sms * 16u ? 8 : 12);
   int order_launches = 0;

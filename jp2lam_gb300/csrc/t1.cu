@@ -555,8 +555,11 @@ __device__ __forceinline__ uint32_t chunk_sym(const uint4& q, int i) {
 }
 
 // Codes all 16 symbols of a chunk, the next symbol's context entry loaded
-// one step ahead of its use.
-__device__ __forceinline__ void mq_chunk16(Mq& m, uint2* ce, const uint2* T, const uint4 q) {
+// one step ahead of its use, capturing numbytes() after symbols e0 - 1 and
+// e1 - 1 (pass ends; outside 1..16 they capture nothing) with predicated
+// selects, so lanes of a warp at different pass ends stay converged.
+__device__ __forceinline__ void mq_chunk16_at(Mq& m, uint2* ce, const uint2* T, const uint4 q, int e0,
+                                              int e1, uint32_t& p0, uint32_t& p1) {
   uint32_t sym = q.x & 0xffu;
   uint2 e = ce[32 * (sym >> 1)];
   #pragma unroll
@@ -569,17 +572,8 @@ __device__ __forceinline__ void mq_chunk16(Mq& m, uint2* ce, const uint2* T, con
     if (cxn == cx) en = ne;
     e = en;
     sym = symn;
-  }
-}
-
-// Codes symbols [from, to) of a chunk one at a time (chunks that hold a pass
-// end or the end of the stream).
-__device__ __forceinline__ void mq_chunk_part(Mq& m, uint2* ce, const uint2* T, const uint4 q,
-                                              int from, int to) {
-  for (int i = from; i < to; ++i) {
-    const uint32_t sym = chunk_sym(q, i);
-    const uint32_t cx = sym >> 1;
-    ce[32 * cx] = mq_step(m, ce[32 * cx], sym, T);
+    p0 = e0 == i + 1 ? (uint32_t)m.pos : p0;
+    p1 = e1 == i + 1 ? (uint32_t)m.pos : p1;
   }
 }
 
@@ -616,51 +610,82 @@ __device__ __forceinline__ void mq_code_block(const T1Args& a, uint32_t b, uint2
   const uint32_t base = a.plane_base[b];
   int pi = 0;
   uint32_t nsym = 0;
-  for (int j = 0; j < mbp; ++j) {
-    // item j codes bit-plane mbp-1-j: SP | MR | CL, or CL alone for j = 0
-    const ItemRec r = a.item_rec[base + j];
+  // One flat loop over the chunks of all items (bit-planes), so lanes of a
+  // warp coding different blocks stay in the same code; the next item's
+  // record and first chunks are fetched during the current item's last
+  // chunk.
+  ItemRec r = a.item_rec[base];
+  ItemRec rn = mbp > 1 ? a.item_rec[base + 1] : r;
+  const uint4* src = reinterpret_cast<const uint4*>(a.sym + (size_t)base * a.sym_slot);
+  uint4 c0 = src[0], c1 = src[1], c2 = src[2];  // the slot and buffer are padded for these reads
+  uint4 n0 = c0, n1 = c0, n2 = c0;
+  int j = 0, lo = 0, kp = 0;
+  auto item_total = [](const ItemRec& x) { return (int)(x.n_sp + x.n_mr + x.n_cl); };
+  // pass ends of item j: SP | MR | CL, or CL alone for the first item
+  auto end_of = [&](int k) {
+    if (j == 0) return item_total(r);
+    return k == 0 ? (int)r.n_sp : (k == 1 ? (int)(r.n_sp + r.n_mr) : item_total(r));
+  };
+  auto record = [&](int k, uint32_t pos) {  // numbytes() after pass k
     const uint8_t bp = (uint8_t)r.bitplane;
-    const int total = (int)(r.n_sp + r.n_mr + r.n_cl);
-    const int npass = j == 0 ? 1 : 3;
-    nsym += (uint32_t)total;
-    int end[3];  // symbol index at which each pass ends
-    end[0] = j == 0 ? total : (int)r.n_sp;
-    end[1] = (int)(r.n_sp + r.n_mr);
-    end[2] = total;
-    auto snapshot = [&](int k) {  // numbytes() after pass k
-      if (npass == 1 || k == 2)
-        pr[pi++] = PassRec{(uint32_t)m.pos, r.ns_cl, j == 0 ? 0u : r.sig_before + r.ns_sp, 2, bp, 0};
-      else if (k == 0)
-        pr[pi++] = PassRec{(uint32_t)m.pos, r.ns_sp, r.sig_before, 0, bp, 0};
-      else
-        pr[pi++] = PassRec{(uint32_t)m.pos, 0u, r.sig_before, 1, bp, 0};
-    };
-    int k = 0;  // next pass to close
-    while (k < npass - 1 && end[k] == 0) snapshot(k++);
-    const uint4* src = reinterpret_cast<const uint4*>(a.sym + (size_t)(base + j) * a.sym_slot);
-    const int nch = (total + 15) >> 4;
-    uint4 c0 = src[0], c1 = src[1], c2 = src[2];
-    for (int ch = 0; ch < nch; ++ch) {
-      const uint4 cur = c0;
-      c0 = c1;
-      c1 = c2;
-      c2 = src[ch + 3];  // 48 bytes ahead: inside the slot or the buffer's 64-byte pad
-      const int lo = ch << 4, hi = lo + 16;
-      if (hi <= total && (k == npass - 1 || end[k] >= hi)) {
-        mq_chunk16(m, ce, T, cur);  // no pass ends inside the chunk
-      } else {
-        const int lim = min(hi, total);
-        for (int at = lo; at < lim;) {
-          const int stop = k == npass - 1 ? lim : min(lim, end[k]);
-          mq_chunk_part(m, ce, T, cur, at - lo, stop - lo);
-          at = stop;
-          while (k < npass - 1 && end[k] == at) snapshot(k++);
-        }
-        continue;
-      }
-      while (k < npass - 1 && end[k] == hi) snapshot(k++);
+    if (j == 0 || k == 2)
+      pr[pi] = PassRec{pos, r.ns_cl, j == 0 ? 0u : r.sig_before + r.ns_sp, 2, bp, 0};
+    else if (k == 0)
+      pr[pi] = PassRec{pos, r.ns_sp, r.sig_before, 0, bp, 0};
+    else
+      pr[pi] = PassRec{pos, 0u, r.sig_before, 1, bp, 0};
+    ++pi;
+  };
+  int npass = 1, total = item_total(r);
+  nsym = (uint32_t)total;
+  for (;;) {
+    // passes of item j that end at its first symbol
+    while (kp < npass - 1 && end_of(kp) == lo) record(kp++, (uint32_t)m.pos);
+    const int cnt = min(16, total - lo);
+    const bool last = lo + cnt >= total;
+    if (last && j + 1 < mbp) {
+      const uint4* ns = reinterpret_cast<const uint4*>(a.sym + (size_t)(base + j + 1) * a.sym_slot);
+      n0 = ns[0];
+      n1 = ns[1];
+      n2 = ns[2];
     }
-    snapshot(npass == 1 ? 0 : 2);
+    const uint4 q = c0;
+    c0 = c1;
+    c1 = c2;
+    c2 = src[(lo >> 4) + 3];  // 48 bytes ahead: inside the slot or the buffer's pad
+    const int e0 = kp < npass - 1 ? end_of(kp) - lo : -1;
+    const int e1 = kp + 1 < npass - 1 ? end_of(kp + 1) - lo : -1;
+    uint32_t p0 = 0, p1 = 0;
+    if (cnt == 16) {
+      mq_chunk16_at(m, ce, T, q, e0, e1, p0, p1);
+    } else {
+      for (int i = 0; i < cnt; ++i) {
+        const uint32_t sym = chunk_sym(q, i);
+        const uint32_t cx = sym >> 1;
+        ce[32 * cx] = mq_step(m, ce[32 * cx], sym, T);
+        p0 = e0 == i + 1 ? (uint32_t)m.pos : p0;
+        p1 = e1 == i + 1 ? (uint32_t)m.pos : p1;
+      }
+    }
+    if (e0 >= 1 && e0 <= cnt) {
+      record(kp++, p0);
+      if (e1 >= 1 && e1 <= cnt) record(kp++, p1);
+    }
+    lo += cnt;
+    if (!last) continue;
+    record(npass == 1 ? 0 : 2, (uint32_t)m.pos);  // cleanup: the item's last pass
+    if (++j == mbp) break;
+    r = rn;
+    if (j + 1 < mbp) rn = a.item_rec[base + j + 1];
+    src = reinterpret_cast<const uint4*>(a.sym + (size_t)(base + j) * a.sym_slot);
+    c0 = n0;
+    c1 = n1;
+    c2 = n2;
+    lo = 0;
+    kp = 0;
+    npass = 3;
+    total = item_total(r);
+    nsym += (uint32_t)total;
   }
   mq_flush(m);
   o.payload_len = (uint32_t)(m.last == 0xffu ? m.pos - 1 : m.pos);  // take_bytes
@@ -1032,13 +1057,14 @@ void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st) {
 }
 
 int mq_blocks_per_warp(const T1Args& a, int num_sms, int bpw) {
-  // Automatic: each warp is a latency-bound chain that issues about once
-  // every five cycles, so about 16 warps per SM keep its schedulers busy;
-  // pack as few blocks per warp as gives that many warps (lanes of a warp
-  // diverge, so fewer blocks per warp is faster while warps are plentiful).
+  // Automatic: up to 16 blocks per SM, one block per warp (the caller pulls
+  // or pipelines them); beyond that, as few blocks per warp (at least 2) as
+  // keep about 24 latency-bound warps per SM, since the lanes of a warp
+  // diverge.
   if (bpw <= 0 || bpw > 32) {
-    const uint32_t target = (uint32_t)num_sms * 16u;
-    bpw = (int)std::min<uint32_t>(32u, std::max<uint32_t>(1u, (a.nblocks + target - 1) / target));
+    const uint32_t sms = (uint32_t)num_sms;
+    if (a.nblocks <= sms * 16u) return 1;
+    bpw = (int)std::min<uint32_t>(32u, std::max<uint32_t>(2u, (a.nblocks + sms * 24u - 1) / (sms * 24u)));
   }
   return bpw;
 }
