@@ -437,7 +437,8 @@ def main():
     kernels = {
         "dwt": ("dwt_batch_kernel (all levels)", dwt_bytes, st_mean["dwt"]),
         "t1_model": ("t1_model_kernel", model_bytes, st_mean["t1_model"]),
-        "t1_mq": ("t1_mq_kernel", mq_bytes, st_mean["t1_mq"]),
+        # one page's blocks are coded by producer/consumer warp pairs
+        "t1_mq": ("t1_mq_pipe_kernel", mq_bytes, st_mean["t1_mq"]),
     }
     def gbs(k):
         _, b, ms = kernels[k]
