@@ -90,7 +90,7 @@ struct jp2g_ctx {
   std::mutex errmu;
   std::mutex mu;    // device pools and stream: one wave (or encode) at a time
   // device pools
-  DevBuf px, ll0, ll1, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
+  DevBuf px, ll0, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
       hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym, stats, dwtargs,
       dwtbases, mqorder, mqscratch;
   // pinned host staging
@@ -425,13 +425,23 @@ struct Prestaged {
 };
 constexpr size_t kStageFailed = ~size_t(0);
 
-// Copies the host pixels of the valid pages among jobs into `buf` (pinned,
-// grown as needed), interleaving planar RGB (Image::from_rgb_bytes takes
-// RGBRGB), and sets each page's px_off. The copy is split into 2 MiB tasks
-// over the host threads. Returns the bytes staged, or kStageFailed.
+// Lays out the host pixels of the valid pages among jobs in the wave's
+// device pixel buffer (sets each page's px_off; returns the bytes, or
+// kStageFailed). Small pages already in the device layout (gray,
+// interleaved RGB) are later copied straight from the caller's memory; the
+// others are copied into `buf` (pinned, at the same offsets), planar RGB
+// interleaved on the way (Image::from_rgb_bytes takes RGBRGB), in 2 MiB
+// tasks over the host threads.
+// Planar RGB must be interleaved on the way; pages above 32 MiB are copied
+// faster by the host threads into pinned memory than by one pageable copy.
+constexpr size_t kDirectCopyMax = 32u << 20;
+bool needs_staging(const PageJob* j) {
+  return (j->ncomp == 3 && !j->interleaved) || (size_t)j->w * j->h * j->ncomp > kDirectCopyMax;
+}
+
 size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
   size_t total = 0;
-  std::vector<PageJob*> host;
+  std::vector<PageJob*> staged;
   for (size_t i = 0; i < n; ++i) {
     PageJob* j = jobs[i];
     PagePlan p;
@@ -439,9 +449,9 @@ size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
     if (!j->host_px || !build_plan(j->w, j->h, (int)j->ncomp, j->quality, j->format, &p, &f)) continue;
     j->px_off = total;
     total += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
-    host.push_back(j);
+    if (needs_staging(j)) staged.push_back(j);
   }
-  if (total == 0) return 0;
+  if (staged.empty()) return total;
   if (!reserve_host(c, buf, total)) return kStageFailed;
   uint8_t* staging = reinterpret_cast<uint8_t*>(buf.p);
   struct CopyTask {
@@ -449,11 +459,11 @@ size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
     size_t p0, p1;  // pixel range
   };
   std::vector<CopyTask> tasks;
-  for (const PageJob* j : host) {
+  for (const PageJob* j : staged) {
     const size_t np = (size_t)j->w * j->h, step = std::max<size_t>((2u << 20) / j->ncomp, 1);
     for (size_t p0 = 0; p0 < np; p0 += step) tasks.push_back({j, p0, std::min(np, p0 + step)});
   }
-  parallel_for(tasks.size(), total > (4u << 20) ? host_threads(c) : 1, [&](size_t k) {
+  parallel_for(tasks.size(), tasks.size() > 2 ? host_threads(c) : 1, [&](size_t k) {
     const CopyTask& t = tasks[k];
     const PageJob* j = t.j;
     uint8_t* dst = staging + j->px_off;
@@ -468,6 +478,7 @@ size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
       std::memcpy(dst + t.p0 * j->ncomp, j->host_px + t.p0 * j->ncomp, (t.p1 - t.p0) * j->ncomp);
     }
   });
+
   return total;
 }
 
@@ -560,9 +571,16 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
     staging = reinterpret_cast<const uint8_t*>(c->hpx.p);
   }
   if (hpx_total > 0) {
-    if (!reserve(c, c->px, hpx_total) ||
-        !cuda_ok(c, cudaMemcpyAsync(c->px.p, staging, hpx_total, cudaMemcpyHostToDevice, c->stream), "H2D"))
-      return kEncodeFailed;
+    if (!reserve(c, c->px, hpx_total)) return kEncodeFailed;
+    // one copy per page: from pinned staging, or straight from the caller's
+    // memory for small pages in the device layout
+    for (PageJob* j : live) {
+      if (!j->host_px) continue;
+      const uint8_t* from = needs_staging(j) ? staging + j->px_off : j->host_px;
+      if (!cuda_ok(c, cudaMemcpyAsync(dptr<uint8_t>(c->px) + j->px_off, from, (size_t)j->w * j->h * j->ncomp,
+                                      cudaMemcpyHostToDevice, c->stream), "H2D"))
+        return kEncodeFailed;
+    }
   }
   if (!cuda_ok(c, cudaMemcpyAsync(c->blocks.p, blocks.data(), nb * sizeof(BlockDesc),
                                   cudaMemcpyHostToDevice, c->stream), "H2D blocks") ||
@@ -873,7 +891,7 @@ void jp2g_destroy(jp2g_ctx* c) {
   if (c->finisher.joinable()) c->finisher.join();
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
-  DevBuf* bufs[] = {&c->px, &c->ll0, &c->ll1, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
+  DevBuf* bufs[] = {&c->px, &c->ll0, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
                     &c->itemrec, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases, &c->mqorder,

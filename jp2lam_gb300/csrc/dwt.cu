@@ -444,12 +444,6 @@ __device__ __forceinline__ void dwt_tile(const DwtLevelArgs& args, int comp, int
   }
 }
 
-template <bool REV>
-__global__ void __launch_bounds__(RT) dwt_tile_kernel(DwtLevelArgs a) {
-  __shared__ typename Cfg<REV>::T s[RSH * RP];
-  dwt_tile<REV>(a, blockIdx.z, blockIdx.x * TW, blockIdx.y * TH, s);
-}
-
 // Flat tile list over many pages: the CTA finds its page by binary search
 // over the tile bases, then its component and tile position.
 template <bool REV>
@@ -486,13 +480,9 @@ void launch_dwt_batch(const DwtLevelArgs* d_args, const uint32_t* d_tile_base, u
 }
 
 void launch_dwt_level(const DwtLevelArgs& a, bool reversible, cudaStream_t st) {
+  // zero levels, or a one-sample-wide/high region (its own scaling rules);
+  // every other level goes through launch_dwt_batch
   dim3 grid((a.rw + TW - 1) / TW, (a.rh + TH - 1) / TH, a.ncomp);
-  if (!a.no_transform && a.rw >= 2 && a.rh >= 2) {
-    if (reversible) dwt_tile_kernel<true><<<grid, RT, 0, st>>>(a);
-    else dwt_tile_kernel<false><<<grid, RT, 0, st>>>(a);
-    return;
-  }
-  // zero levels, or a one-sample-wide/high region (its own scaling rules)
   if (reversible) dwt_level_kernel<true><<<grid, NT, 0, st>>>(a);
   else dwt_level_kernel<false><<<grid, NT, 0, st>>>(a);
 }

@@ -33,6 +33,8 @@ struct DwtLevelArgs {
   DwtBandOut band[3][4];
 };
 
+// One level of one page with the shared-memory lifting kernel: used for
+// pages with no decomposition level and regions under 2 samples wide or high.
 void launch_dwt_level(const DwtLevelArgs& a, bool reversible, cudaStream_t st);
 
 // One level of many pages in one launch: d_args[i] describes page i's level
