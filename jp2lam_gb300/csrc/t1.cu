@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(kModelWarps * 32, 3) t1_model_kernel(T1Args a)
         // emission in scan order: within the stripe column by column (each
         // lane: its column xa, then xb), rows top to bottom
         const uint64_t F0 = S0 | N0, F1 = S1 | N1, F2 = S2 | N2, F3 = S3 | N3;
-        {
+        if (V0 | V1 | V2 | V3) {  // same masks in every lane: a uniform skip of empty stripes
           const uint32_t wfp = win4(Fp, sh), wd = win4(D, sh);
           const uint32_t wf[4] = {win4(F0, sh), win4(F1, sh), win4(F2, sh), win4(F3, sh)};
           const uint32_t wp[4] = {win4(S0, sh), win4(S1, sh), win4(S2, sh), win4(S3, sh)};
@@ -307,6 +307,7 @@ __global__ void __launch_bounds__(kModelWarps * 32, 3) t1_model_kernel(T1Args a)
       __syncwarp();
       // ---- magnitude refinement ----
       for (int k = 0; k < h; k += 4) {
+        if (!(s.S[k + 1] | s.S[k + 2] | s.S[k + 3] | s.S[k + 4])) continue;  // nothing to refine
         uint32_t wf[6];  // state after SP of rows k-1 .. k+4
         #pragma unroll
         for (int r = 0; r < 6; ++r) wf[r] = win4(s.S[k + r] | s.N[k + r], sh);
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(kModelWarps * 32, 3) t1_model_kernel(T1Args a)
                          eastm(Gr[0] | Gr[1] | Gr[2] | Gr[3]) | dil(Gd);
           clean = ~(busy | nbr) & valid;
         }
-        {
+        if (Cr[0] | Cr[1] | Cr[2] | Cr[3]) {  // any sample left to code in this stripe
           const uint32_t wgp = win4(Gp, sh), wgd = win4(Gd, sh), wcl = win4(clean, sh);
           uint32_t wG[4], wF[4], wC[4], wB[4], wsg[6];
           #pragma unroll
