@@ -832,10 +832,12 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
   load_fat_table(F);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int pipe = warp >> 1;
+  // producers are warps 0..kPipes-1 and consumers the warps above, so the
+  // (heavier) producer chains spread over the SM's schedulers
+  const int pipe = warp % kPipes;
   const int bar = 1 + pipe;
   PipeChunk* slot = slots[pipe];
-  if ((warp & 1) == 0) {
+  if (warp < kPipes) {
     // ---- producer: interval and state chain ----
     uint32_t* ci = ci_all[pipe];
     uint32_t b = kPipeEnd, base = 0, A = 0x8000u;
