@@ -237,6 +237,16 @@ void build_tables(const PagePlan& p, uint32_t block_base, uint32_t band_base, ui
 // Arguments of decomposition level l (1 = first) of a page whose pixels are
 // at d_px; llA/llB are the page's two LL planes (level l writes its LL to
 // llA when l is odd, to llB when even, and reads the other).
+// Samples per row of an intermediate LL plane: a multiple of 16, so the tile
+// kernel stores each 16-sample run as aligned 16-byte vectors within the row.
+size_t ll_pitch(int width) { return ((size_t)width + 15) & ~size_t(15); }
+
+// Samples of each of a page's two LL planes (the first level's LL is the
+// largest), rounded to 64 so both planes stay 256-byte aligned.
+size_t ll_plane_elems(const PagePlan& p) {
+  return (ll_pitch((p.width + 1) / 2) * (size_t)((p.height + 1) / 2) * p.ncomp + 63) & ~size_t(63);
+}
+
 DwtLevelArgs level_args(const PagePlan& p, int l, const uint8_t* d_px, uint32_t block_base,
                         int32_t* coef, void* llA, void* llB) {
   DwtLevelArgs a{};
@@ -252,7 +262,7 @@ DwtLevelArgs level_args(const PagePlan& p, int l, const uint8_t* d_px, uint32_t 
     a.px_pitch = (size_t)p.width * p.ncomp;
   } else {
     a.src = (l - 1) % 2 ? llA : llB;
-    a.src_pitch = (size_t)p.ladder[res].first;
+    a.src_pitch = ll_pitch(p.ladder[res].first);
     a.src_comp = a.src_pitch * (size_t)p.ladder[res].second;
   }
   a.coef = coef;
@@ -273,7 +283,7 @@ DwtLevelArgs level_args(const PagePlan& p, int l, const uint8_t* d_px, uint32_t 
     band_out(0);
   } else {
     a.ll = l % 2 ? llA : llB;
-    a.ll_pitch = (size_t)p.ladder[res - 1].first;
+    a.ll_pitch = ll_pitch(p.ladder[res - 1].first);
     a.ll_comp = a.ll_pitch * (size_t)p.ladder[res - 1].second;
   }
   return a;
@@ -292,9 +302,8 @@ int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live) {
     const PagePlan& p = live[i]->plan;
     maxL = std::max(maxL, p.levels);
     if (p.levels >= 2) {
-      const size_t e = ((size_t)(p.width + 1) / 2) * ((p.height + 1) / 2) * p.ncomp;
       ll_off[i] = ll_total;
-      ll_total += 2 * ((e + 63) & ~size_t(63));
+      ll_total += 2 * ll_plane_elems(p);
     }
   }
   if (ll_total > 0 && !reserve(c, c->ll0, ll_total * 4)) return kEncodeFailed;
@@ -345,9 +354,7 @@ int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live) {
         const PagePlan& p = live[i]->plan;
         if (p.levels < l || p.lossless != rev) continue;
         int32_t* ll = dptr<int32_t>(c->ll0) + ll_off[i];
-        const size_t half = p.levels >= 2
-            ? (((size_t)(p.width + 1) / 2) * ((p.height + 1) / 2) * p.ncomp + 63) & ~size_t(63)
-            : 0;
+        const size_t half = p.levels >= 2 ? ll_plane_elems(p) : 0;
         DwtLevelArgs a = level_args(p, l, page_px(i), live[i]->block_base, coef, ll, ll + half);
         if (a.rw >= 2 && a.rh >= 2) {
           args.push_back(a);

@@ -256,192 +256,227 @@ __global__ void __launch_bounds__(NT) dwt_level_kernel(DwtLevelArgs a) {
 // ---------------------------------------------------------------------------
 // Register-resident tile kernel (every level with a region of at least 2x2).
 //
-// A CTA of 288 threads owns a TW x TH = 128 x 64 tile plus a 4-sample halo
-// (a 136 x 72 shared-memory tile). Lifting runs on per-thread register
-// arrays of 40 samples (32 outputs plus 4 halo samples on each side, so
-// every lifting step sees its true neighbours):
-//   vertical:   272 jobs = 136 columns x 2 row halves,
-//   horizontal: 256 jobs = 64 rows x 4 column quarters.
-// Lanes take consecutive columns (vertical) or consecutive rows
-// (horizontal); the odd shared-memory pitch keeps both conflict-free. Every
-// job reads its 40 samples before a barrier and writes its 32 outputs after
-// it, so overlapping halos read the pre-step values. The epilogue walks each
-// subband's 64 x 32 part of the tile in row order, applies the column scale
-// (9/7), quantises and stores whole code-block rows.
+// A CTA of 288 threads owns a TW x TH = 128 x 64 tile of the level's input
+// plus a 4-sample border, mirrored at the region edges:
+//   1. vertical: 272 jobs = 136 columns x 2 row halves. A job reads the
+//      samples its 32 outputs depend on straight from global memory (the
+//      page's pixels with the level shift and RCT/ICT applied, or the
+//      previous level's LL plane), lifts them in registers and writes the
+//      32 outputs to shared memory, even tile rows in smem rows 0-31 and odd
+//      ones in rows 32-63.
+//   2. horizontal: 256 jobs = 4 column quarters x 64 rows. The 32 rows of a
+//      warp share one parity (and read 32 consecutive smem rows, odd pitch:
+//      no bank conflict), so a warp produces two subbands, LL/HL from even
+//      rows or LH/HH from odd ones. A job lifts 40 samples of its row,
+//      applies the 9/7 column scale, quantises its 16 low and 16 high
+//      outputs and stores each run as four 16-byte vectors into a
+//      code-block row (or the next LL plane, whose pitch is a multiple of
+//      16 samples). Code-blocks are 32 or 64 wide and runs start at
+//      multiples of 16, so a run never crosses a code-block; samples past
+//      the band edge land in the slot's unused columns (or the plane's
+//      padding), which nothing reads.
+// Lifting runs in wavefront order: a step is applied as soon as the two
+// neighbours it reads are final, so samples leave the register set early.
+// Whole-sample symmetric extension commutes with the lifting steps, so every
+// output equals the reference's whole-row/whole-column lifting bit for bit.
 constexpr int RT = 288;
-constexpr int RH = 4;             // halo
+constexpr int RH = 4;             // border
 constexpr int RN = 40;            // samples per register job (32 + 2 * RH)
-constexpr int RSW = TW + 2 * RH;  // 136
-constexpr int RSH = TH + 2 * RH;  // 72
-constexpr int RP = RSW + 1;       // shared-memory pitch
+constexpr int RSW = TW + 2 * RH;  // 136 columns of vertical jobs
+constexpr int RP = RSW + 1;       // shared-memory pitch (odd)
 
-template <bool REV, typename T>
-__device__ __forceinline__ void lift_regs(T (&x)[RN]) {
+// Samples x[LO..HI] of a job are read; they determine outputs x[4..35].
+template <bool REV>
+struct JobRange {
+  static constexpr int LO = REV ? 2 : 0;
+  static constexpr int HI = REV ? 36 : 38;
+};
+
+// Lifts x in wavefront order and hands every output to emit(i, value),
+// i = 4..35, in the order 5, 4, 7, 6, ..., 35, 34.
+template <bool REV, typename T, typename Emit>
+__device__ __forceinline__ void lift_wave(T (&x)[RN], Emit&& emit) {
   if constexpr (REV) {
     // predict on odd samples, update on even ones (rev53.rs:419-497)
     #pragma unroll
-    for (int i = 1; i < RN - 1; i += 2) x[i] -= (x[i - 1] + x[i + 1]) >> 1;
-    #pragma unroll
-    for (int i = 2; i < RN - 1; i += 2) x[i] += (x[i - 1] + x[i + 1] + 2) >> 2;
+    for (int k = 3; k <= 35; k += 2) {
+      x[k] -= (x[k - 1] + x[k + 1]) >> 1;
+      if (k >= 5) {
+        x[k - 1] += (x[k - 2] + x[k] + 2) >> 2;
+        emit(k, x[k]);
+        emit(k - 1, x[k - 1]);
+      }
+    }
   } else {
     // alpha (odd), beta (even), gamma (odd), delta (even) (irrev97.rs:261-336)
     #pragma unroll
-    for (int i = 1; i < RN - 1; i += 2) x[i] = lift97(x[i], kAlpha, x[i - 1], x[i + 1]);
-    #pragma unroll
-    for (int i = 2; i < RN - 2; i += 2) x[i] = lift97(x[i], kBeta, x[i - 1], x[i + 1]);
-    #pragma unroll
-    for (int i = 3; i < RN - 2; i += 2) x[i] = lift97(x[i], kGamma, x[i - 1], x[i + 1]);
-    #pragma unroll
-    for (int i = 4; i < RN - 4; i += 2) x[i] = lift97(x[i], kDelta, x[i - 1], x[i + 1]);
+    for (int k = 1; k <= 37; k += 2) {
+      x[k] = lift97(x[k], kAlpha, x[k - 1], x[k + 1]);
+      if (k >= 3) x[k - 1] = lift97(x[k - 1], kBeta, x[k - 2], x[k]);
+      if (k >= 5) x[k - 2] = lift97(x[k - 2], kGamma, x[k - 3], x[k - 1]);
+      if (k >= 7) {
+        x[k - 3] = lift97(x[k - 3], kDelta, x[k - 4], x[k - 2]);
+        emit(k - 2, x[k - 2]);
+        emit(k - 3, x[k - 3]);
+      }
+    }
   }
 }
 
-// One value of the level's input: the page's pixels (level shift and
-// RCT/ICT applied) or the previous level's LL plane.
-template <bool REV>
-struct TileSrc {
+// b - 128 as a float, exactly: the bits of 2^23 + b minus 2^23 + 128.
+__device__ __forceinline__ float byte_centered(uint32_t b) {
+  return __fsub_rn(__uint_as_float(0x4B000000u | b), 8388736.0f);
+}
+
+// One column of the level's input. KIND 0: the previous LL plane; 1: pixels,
+// one byte per sample; 2: three interleaved bytes through RCT/ICT.
+template <bool REV, int KIND>
+struct ColumnSrc {
   using T = typename Cfg<REV>::T;
-  const uint8_t* px;
-  size_t px_pitch;
-  const T* ll;
-  size_t ll_pitch;
-  int ncomp, comp, mct, from_pixels;
-  __device__ __forceinline__ T at(int gx, int gy) const {
-    if (from_pixels) {
-      const uint8_t* row = px + (size_t)gy * px_pitch;
-      if (!mct) return (T)((int)row[(size_t)gx * ncomp + comp] - 128);
-      const uint8_t* q = row + (size_t)gx * 3;
-      const int r = (int)q[0] - 128, g = (int)q[1] - 128, b = (int)q[2] - 128;
+  const uint8_t* px;  // KIND 1, 2: the column's first byte in row 0
+  const T* ll;        // KIND 0: the column's sample in row 0
+  size_t pitch;       // bytes (pixels) or samples (LL plane) per row
+  int comp;
+  float c0, c1, c2;   // the component's ICT row (KIND 2, irreversible)
+  __device__ __forceinline__ T operator()(int gy) const {
+    if constexpr (KIND == 0) {
+      return ll[(size_t)gy * pitch];
+    } else if constexpr (KIND == 1) {
+      const uint32_t b = px[(size_t)gy * pitch];
+      if constexpr (REV) return (int)b - 128;
+      else return byte_centered(b);
+    } else {
+      const uint8_t* q = px + (size_t)gy * pitch;
+      const uint32_t r8 = q[0], g8 = q[1], b8 = q[2];
       if constexpr (REV) {  // RCT (src/simd/scalar.rs:173-195)
-        return (T)(comp == 0 ? ((r + 2 * g + b) >> 2) : (comp == 1 ? b - g : r - g));
+        const int r = (int)r8 - 128, g = (int)g8 - 128, b = (int)b8 - 128;
+        return comp == 0 ? ((r + 2 * g + b) >> 2) : (comp == 1 ? b - g : r - g);
       } else {  // ICT (src/simd/scalar.rs:149-171), evaluated left to right
-        const float rf = (float)r, gf = (float)g, bf = (float)b;
-        if (comp == 0)
-          return __fadd_rn(__fadd_rn(__fmul_rn(0.299f, rf), __fmul_rn(0.587f, gf)), __fmul_rn(0.114f, bf));
-        if (comp == 1)
-          return __fadd_rn(__fadd_rn(__fmul_rn(-0.16875f, rf), __fmul_rn(-0.33126f, gf)), __fmul_rn(0.5f, bf));
-        return __fsub_rn(__fsub_rn(__fmul_rn(0.5f, rf), __fmul_rn(0.41869f, gf)), __fmul_rn(0.08131f, bf));
+        return __fadd_rn(__fadd_rn(__fmul_rn(c0, byte_centered(r8)), __fmul_rn(c1, byte_centered(g8))),
+                         __fmul_rn(c2, byte_centered(b8)));
       }
     }
-    return ll[(size_t)gy * ll_pitch + gx];
   }
 };
 
+// Vertical job: rows y_first + LO .. y_first + HI of one column, lifted, the
+// 32 outputs (9/7: scaled 1/K on even rows, K on odd ones) written to col.
+template <bool REV, int KIND>
+__device__ __forceinline__ void vertical_job(const ColumnSrc<REV, KIND>& src, int y_first, int rh,
+                                             typename Cfg<REV>::T* col) {
+  using T = typename Cfg<REV>::T;
+  constexpr int LO = JobRange<REV>::LO, HI = JobRange<REV>::HI;
+  T x[RN];
+  if (y_first + LO >= 0 && y_first + HI < rh) {
+    #pragma unroll
+    for (int i = LO; i <= HI; ++i) x[i] = src(y_first + i);
+  } else {
+    #pragma unroll
+    for (int i = LO; i <= HI; ++i) x[i] = src(sym(y_first + i, rh));
+  }
+  lift_wave<REV>(x, [&](int i, T v) {
+    if constexpr (!REV) v = __fmul_rn(v, (i & 1) ? kK : kInvK);
+    col[((i & 1) * 32 + ((i - 4) >> 1)) * RP] = v;
+  });
+}
+
+__device__ __forceinline__ void store_run(uint32_t* dst, const uint32_t (&v)[16]) {
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  #pragma unroll
+  for (int m = 0; m < 4; ++m) d[m] = make_uint4(v[4 * m], v[4 * m + 1], v[4 * m + 2], v[4 * m + 3]);
+}
+
+// First sample of code-block row v, column u (a multiple of 16) of a band.
+__device__ __forceinline__ uint32_t* slot_at(int32_t* coef, const DwtBandOut& b, int v, int u, int cbs,
+                                             int cbhs) {
+  const uint32_t blk = b.first_block + (uint32_t)(v >> cbhs) * b.ncbx + (uint32_t)(u >> cbs);
+  return reinterpret_cast<uint32_t*>(coef + ((size_t)blk << (cbs + cbhs)) +
+                                     ((size_t)(v & ((1 << cbhs) - 1)) << cbs) + (u & ((1 << cbs) - 1)));
+}
+
 // One tile of one level (see the comment above RT). The level's arguments
-// are read once into registers: the caller's copy may live in global memory.
+// are read as needed: the caller's copy lives in global memory.
 template <bool REV>
 __device__ __forceinline__ void dwt_tile(const DwtLevelArgs& args, int comp, int x0, int y0,
                                          typename Cfg<REV>::T* s) {
   using T = typename Cfg<REV>::T;
+  constexpr int LO = JobRange<REV>::LO, HI = JobRange<REV>::HI;
   const int rw = args.rw, rh = args.rh;
   const int tid = threadIdx.x;
-  TileSrc<REV> src;
-  src.from_pixels = args.from_pixels;
-  src.px = args.px;
-  src.px_pitch = args.px_pitch;
-  src.ncomp = args.ncomp;
-  src.comp = comp;
-  src.mct = args.mct;
-  src.ll = reinterpret_cast<const T*>(args.src) + (size_t)comp * args.src_comp;
-  src.ll_pitch = args.src_pitch;
+
+  // ---- 1. vertical jobs: column lx, rows [32 h, 32 h + 40) of the tile ----
+  if (tid < 2 * RSW) {
+    const int h = tid >= RSW ? 1 : 0, lx = tid - h * RSW;
+    int gx = x0 - RH + lx;
+    if ((unsigned)gx >= (unsigned)rw) gx = sym(gx, rw);
+    const int y_first = y0 - RH + 32 * h;
+    T* col = s + 16 * h * RP + lx;
+    if (!args.from_pixels) {
+      ColumnSrc<REV, 0> src{};
+      src.ll = reinterpret_cast<const T*>(args.src) + (size_t)comp * args.src_comp + gx;
+      src.pitch = args.src_pitch;
+      vertical_job<REV, 0>(src, y_first, rh, col);
+    } else if (!args.mct) {
+      ColumnSrc<REV, 1> src{};
+      src.px = args.px + (size_t)gx * args.ncomp + comp;
+      src.pitch = args.px_pitch;
+      vertical_job<REV, 1>(src, y_first, rh, col);
+    } else {
+      ColumnSrc<REV, 2> src{};
+      src.px = args.px + (size_t)gx * 3;
+      src.pitch = args.px_pitch;
+      src.comp = comp;
+      src.c0 = comp == 0 ? 0.299f : comp == 1 ? -0.16875f : 0.5f;
+      src.c1 = comp == 0 ? 0.587f : comp == 1 ? -0.33126f : -0.41869f;
+      src.c2 = comp == 0 ? 0.114f : comp == 1 ? 0.5f : -0.08131f;
+      vertical_job<REV, 2>(src, y_first, rh, col);
+    }
+  }
+  __syncthreads();
+
+  // ---- 2. horizontal jobs: tile row 2 lane + p, columns [32 q, 32 q + 40) ----
+  const int warp = tid >> 5, lane = tid & 31;
+  if (warp >= 8) return;
+  const int p = warp & 1, q = warp >> 1;
+  const T* row = s + (p * 32 + lane) * RP + 32 * q;
+  T x[RN];
+  #pragma unroll
+  for (int i = LO; i <= HI; ++i) x[i] = row[i];
+
+  const int cbs = __ffs(args.cbw) - 1, cbhs = __ffs(args.cbh) - 1;
+  const int v = (y0 >> 1) + lane;  // band row
+  const int u = (x0 >> 1) + 16 * q;  // first band column of both runs
+  const bool row_ok = y0 + 2 * lane + p < rh;
+  const bool lo_ok = row_ok && u < ((rw + 1) >> 1), hi_ok = row_ok && u < (rw >> 1);
   T* const ll_out = args.ll ? reinterpret_cast<T*>(args.ll) + (size_t)comp * args.ll_comp : nullptr;
-  const size_t ll_pitch = args.ll_pitch;
-  int32_t* const coef = args.coef;
-  const int cbw = args.cbw, cbh = args.cbh;
-
-  // ---- load tile + halo (mirrored at the region borders) ----
-  {
-    const int tx = tid & 31, ty = tid >> 5, nty = RT / 32;
-    const bool inner_x = x0 - RH >= 0 && x0 - RH + RSW <= rw;
-    for (int ly = ty; ly < RSH; ly += nty) {
-      int gy = y0 - RH + ly;
-      if ((unsigned)gy >= (unsigned)rh) gy = sym(gy, rh);
-      for (int lx = tx; lx < RSW; lx += 32) {
-        int gx = x0 - RH + lx;
-        if (!inner_x && (unsigned)gx >= (unsigned)rw) gx = sym(gx, rw);
-        s[ly * RP + lx] = src.at(gx, gy);
+  const DwtBandOut bhi = args.band[comp][p ? 3 : 1];  // HL or HH
+  uint32_t lo[16], hi[16];
+  if (p == 0 && ll_out != nullptr) {
+    // even rows of an intermediate level: LL to the next plane, unquantised
+    lift_wave<REV>(x, [&](int i, T val) {
+      if (i & 1) {
+        if constexpr (REV) hi[(i - 5) >> 1] = (uint32_t)val;
+        else hi[(i - 5) >> 1] = (uint32_t)quantize(__fmul_rn(val, kK), bhi.step);
+      } else {
+        if constexpr (REV) lo[(i - 4) >> 1] = (uint32_t)val;
+        else lo[(i - 4) >> 1] = __float_as_uint(__fmul_rn(val, kInvK));
       }
-    }
-  }
-  __syncthreads();
-
-  // ---- vertical lifting: column lx, rows [32 h, 32 h + 40) ----
-  {
-    T x[RN];
-    const int job = tid;  // 272 jobs, 288 threads
-    const bool active = job < 2 * RSW;
-    const int h = job >= RSW ? 1 : 0, lx = job - h * RSW, r0 = 32 * h;
-    if (active) {
-      #pragma unroll
-      for (int i = 0; i < RN; ++i) x[i] = s[(r0 + i) * RP + lx];
-    }
-    __syncthreads();
-    if (active) {
-      lift_regs<REV>(x);
-      #pragma unroll
-      for (int i = RH; i < RN - RH; ++i) {
-        T v = x[i];
-        if constexpr (!REV) v = __fmul_rn(v, (i & 1) ? kK : kInvK);  // rows: 1/K even, K odd
-        s[(r0 + i) * RP + lx] = v;
+    });
+    if (lo_ok) store_run(reinterpret_cast<uint32_t*>(ll_out + (size_t)v * args.ll_pitch + u), lo);
+  } else {
+    const DwtBandOut blo = args.band[comp][p ? 2 : 0];  // LL (last level) or LH
+    lift_wave<REV>(x, [&](int i, T val) {
+      if (i & 1) {
+        if constexpr (REV) hi[(i - 5) >> 1] = (uint32_t)val;
+        else hi[(i - 5) >> 1] = (uint32_t)quantize(__fmul_rn(val, kK), bhi.step);
+      } else {
+        if constexpr (REV) lo[(i - 4) >> 1] = (uint32_t)val;
+        else lo[(i - 4) >> 1] = (uint32_t)quantize(__fmul_rn(val, kInvK), blo.step);
       }
-    }
+    });
+    if (lo_ok) store_run(slot_at(args.coef, blo, v, u, cbs, cbhs), lo);
   }
-  __syncthreads();
-
-  // ---- horizontal lifting: row RH + r, columns [32 q, 32 q + 40) ----
-  {
-    T x[RN];
-    const int job = tid;  // 256 jobs
-    const bool active = job < 4 * TH;
-    const int q = job / TH, r = job - q * TH, c0 = 32 * q;
-    T* row = s + (RH + r) * RP;
-    if (active) {
-      #pragma unroll
-      for (int i = 0; i < RN; ++i) x[i] = row[c0 + i];
-    }
-    __syncthreads();
-    if (active) {
-      lift_regs<REV>(x);
-      #pragma unroll
-      for (int i = RH; i < RN - RH; ++i) row[c0 + i] = x[i];
-    }
-  }
-  __syncthreads();
-
-  // ---- epilogue: each subband's 64 x 32 part, rows in order ----
-  const int cbs = __ffs(cbw) - 1, cbhs = __ffs(cbh) - 1;
-  const int u0 = x0 >> 1, v0 = y0 >> 1;
-  #pragma unroll 1
-  for (int band = 0; band < 4; ++band) {  // LL, HL, LH, HH
-    const int bw = (band & 1) ? rw >> 1 : (rw + 1) >> 1;
-    const int bh = (band & 2) ? rh >> 1 : (rh + 1) >> 1;
-    const int cols = min(64, bw - u0), rows = min(32, bh - v0);
-    if (cols <= 0 || rows <= 0) continue;
-    const T* sb = s + (RH + (band >> 1)) * RP + RH + (band & 1);
-    const float cscale = (band & 1) ? kK : kInvK;  // columns: 1/K even, K odd (9/7)
-    if (band == 0 && ll_out != nullptr) {
-      for (int idx = tid; idx < 32 * 64; idx += RT) {
-        const int rr = idx >> 6, cc = idx & 63;
-        if (rr >= rows || cc >= cols) continue;
-        T val = sb[2 * rr * RP + 2 * cc];
-        if constexpr (!REV) val = __fmul_rn(val, cscale);
-        ll_out[(size_t)(v0 + rr) * ll_pitch + u0 + cc] = val;
-      }
-      continue;
-    }
-    const DwtBandOut bo = args.band[comp][band];
-    for (int idx = tid; idx < 32 * 64; idx += RT) {
-      const int rr = idx >> 6, cc = idx & 63;
-      if (rr >= rows || cc >= cols) continue;
-      T val = sb[2 * rr * RP + 2 * cc];
-      const int u = u0 + cc, v = v0 + rr;
-      const uint32_t blk = bo.first_block + (uint32_t)(v >> cbhs) * bo.ncbx + (uint32_t)(u >> cbs);
-      int32_t qv;
-      if constexpr (REV) qv = val;
-      else qv = quantize(__fmul_rn(val, cscale), bo.step);
-      coef[((size_t)blk << (cbs + cbhs)) + ((size_t)(v & (cbh - 1)) << cbs) + (u & (cbw - 1))] = qv;
-    }
-  }
+  if (hi_ok) store_run(slot_at(args.coef, bhi, v, u, cbs, cbhs), hi);
 }
 
 // Flat tile list over many pages: the CTA finds its page by binary search
@@ -450,7 +485,7 @@ template <bool REV>
 __global__ void __launch_bounds__(RT) dwt_batch_kernel(const DwtLevelArgs* __restrict__ args,
                                                        const uint32_t* __restrict__ tile_base,
                                                        uint32_t npages) {
-  __shared__ typename Cfg<REV>::T s[RSH * RP];
+  __shared__ typename Cfg<REV>::T s[TH * RP];
   const uint32_t t = blockIdx.x;
   uint32_t lo = 0, hi = npages;  // tile_base[lo] <= t < tile_base[hi]
   while (hi - lo > 1) {
