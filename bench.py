@@ -219,6 +219,12 @@ def bench_batched(eng, stream, torch, dev, args):
     plain_mpix = sum(p["w"] * p["h"] for p in plain_pages) / 1e6
     del bufs
     ms = float(np.mean(dev_t))
+    # colour + DWT + quantisation of the whole batch: 5 algorithmic bytes per
+    # component-sample (1 B pixel read, 4 B int32 coefficient written)
+    dwt_bytes = 5.0 * sum(p["w"] * p["h"] * p["ncomp"] for p in pages)
+    peaks = _peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    dwt_gbs = dwt_bytes / (st["dwt"] * 1e6) if st["dwt"] else None
     return {
         "workload": f"{len(pages)} sRGB 2550x3300 pages (seeds 1000+i, 800x600 photo), quality 75 "
                     "(ICT + 9/7, 6 levels) -> JP2, one jp2g_encode_batch call per step; inputs "
@@ -233,6 +239,10 @@ def bench_batched(eng, stream, torch, dev, args):
                   "sample": "the first 8 pages, one jp2g_encode_device / jp2g_encode each"},
         "speedup_vs_plain": (mpix / (ms / 1e3)) / (plain_mpix / (np.mean(plain_t) / 1e3)),
         "stages_ms": st, "gpu_launches": int(cnt[5]),
+        "roofline_dwt": {"bound": "hbm", "achieved": dwt_gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": dwt_gbs / hbm if dwt_gbs else None,
+                         "algorithmic_bytes_per_batch": dwt_bytes,
+                         "peak_source": "fallback" if peaks.get("fallback") else "measured"},
         "counters": {"code_blocks": int(cnt[0]), "passes": int(cnt[2]), "mq_symbols": int(cnt[7]),
                      "coefficient_bitplanes": int(cnt[6])},
         "t1_rates": {"code_blocks_per_s": cnt[0] / (st["tier1"] / 1e3) if st["tier1"] else None,
