@@ -198,19 +198,45 @@ def _time_calls(fn, steps, warmup, stream, torch):
     return times
 
 
+OPT_NAMES = ["wave_blocks", "mq_blocks_per_warp", "host_threads", "mq_warps_per_sm", "mq_pipes_per_sm",
+             "mq_heavy"]
+
+
+def _autotune(eng, dpages, args):
+    """Runs jp2g_autotune on the workload's own pages (outside any timed
+    region, as a service does at start-up) and returns (defaults, record)."""
+    from jp2lam_gb300 import _native
+    defaults = [eng.get_option(o) for o in range(_native.NUM_OPTS)]
+    if args.no_autotune:
+        return defaults, None
+    t0 = time.perf_counter()
+    best, ms = eng.autotune(dpages, repeats=1)
+    return defaults, {"options": {OPT_NAMES[o]: int(v) for o, v in best.items()},
+                      "best_sample_ms": ms, "seconds": time.perf_counter() - t0,
+                      "sample": "the workload's own pages, device-resident"}
+
+
+def _restore(eng, defaults):
+    for o, v in enumerate(defaults):
+        eng.set_option(o, v)
+
+
 def bench_batched(eng, stream, torch, dev, args):
     """64 sRGB pages per step through jp2g_encode_batch vs one jp2g_encode per
-    page, same pages."""
+    page, same pages. The batch runs under the autotuner's choice; the plain
+    path under the default options."""
     pages = _rgb_pages(args.batch_pages, 1000)
     mpix = sum(p["w"] * p["h"] for p in pages) / 1e6
     bufs, dpages = _to_device(pages, torch, dev)
     torch.cuda.synchronize()
+    defaults, tuned = _autotune(eng, dpages, args)
     sizes = []
     dev_t = _time_calls(lambda: sizes.append(sum(len(o) for o in eng.encode_batch(dpages))),
                         args.batch_steps, 2, stream, torch)
     st = eng.stage_times()
     cnt = eng.counters()
     host_t = _time_calls(lambda: eng.encode_batch(pages), args.batch_steps, 1, stream, torch)
+    _restore(eng, defaults)
     plain_pages = pages[:8]
     plain_t = _time_calls(lambda: [eng.encode_device(p["px"], p["w"], p["h"], p["ncomp"], p["quality"],
                                                      p["fmt"]) for p in dpages[:8]], 2, 1, stream, torch)
@@ -238,6 +264,7 @@ def bench_batched(eng, stream, torch, dev, args):
                   "e2e": plain_mpix / (np.mean(plain_host_t) / 1e3), "unit": "MPix/s",
                   "sample": "the first 8 pages, one jp2g_encode_device / jp2g_encode each"},
         "speedup_vs_plain": (mpix / (ms / 1e3)) / (plain_mpix / (np.mean(plain_t) / 1e3)),
+        "autotune": tuned,
         "stages_ms": st, "gpu_launches": int(cnt[5]),
         "roofline_dwt": {"bound": "hbm", "achieved": dwt_gbs, "peak": hbm, "unit": "GB/s",
                          "frac": dwt_gbs / hbm if dwt_gbs else None,
@@ -255,8 +282,11 @@ def bench_uneven(eng, stream, torch, dev, args):
     mpix = sum(p["w"] * p["h"] for p in pages) / 1e6
     bufs, dpages = _to_device(pages, torch, dev)
     torch.cuda.synchronize()
+    defaults, tuned = _autotune(eng, dpages, args)
     dev_t = _time_calls(lambda: eng.encode_batch(dpages), 3, 2, stream, torch)
+    launches = int(eng.counters()[5])
     host_t = _time_calls(lambda: eng.encode_batch(pages), 3, 2, stream, torch)
+    _restore(eng, defaults)
     plain_t = _time_calls(lambda: [eng.encode_device(p["px"], p["w"], p["h"], p["ncomp"], p["quality"],
                                                      p["fmt"]) for p in dpages], 1, 1, stream, torch)
     del bufs
@@ -266,7 +296,7 @@ def bench_uneven(eng, stream, torch, dev, args):
             "e2e": mpix / (np.mean(host_t) / 1e3),
             "plain": mpix / (np.mean(plain_t) / 1e3),
             "speedup_vs_plain": float(np.mean(plain_t) / np.mean(dev_t)),
-            "gpu_launches": int(eng.counters()[5])}
+            "autotune": tuned, "gpu_launches": launches}
 
 
 def bench_served(jl, local, args):
@@ -342,6 +372,8 @@ def main():
     ap.add_argument("--only-batch", action="store_true",
                     help="run only the batched leg (for profiling); prints its object")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="time the batched and uneven workloads under the default options")
     ap.add_argument("--batch-pages", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--uneven-pages", type=int, default=64)

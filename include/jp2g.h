@@ -107,7 +107,10 @@ int jp2g_submit(jp2g_ctx* ctx, const jp2g_request* req, uint64_t* ticket);
 int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, int timeout_ms);
 
 /* Tuning knobs (the autotuner sets these):
- * JP2G_OPT_WAVE_BLOCKS        most code-blocks per device wave (default 160000);
+ * JP2G_OPT_WAVE_BLOCKS        most code-blocks per device wave (default 160000;
+ *                             waves never exceed 246,723 64x64 blocks or
+ *                             838,860 32x32 blocks, whose payload slots need
+ *                             32-bit offsets);
  * JP2G_OPT_MQ_BLOCKS_PER_WARP code-blocks per warp in MQ coding, 1..32, or 0
  *                             for automatic (1 up to 16 blocks per SM, else
  *                             2..32 for about 24 warps per SM);
@@ -137,6 +140,20 @@ enum {
 };
 int jp2g_set_option(jp2g_ctx* ctx, int option, int64_t value);
 int jp2g_get_option(jp2g_ctx* ctx, int option, int64_t* value);
+
+/* Autotuner: encodes the caller's sample pages (through jp2g_encode_batch)
+ * under each candidate setting of the MQ schedule (automatic; 4, 8 or 16
+ * producer/consumer pairs per SM; 8, 12 or 16 pulling warps per SM; 2 to 32
+ * blocks packed per warp), then of the wave size (20,000 to 240,000
+ * code-blocks) under the fastest schedule, and leaves the fastest setting on
+ * the context. A candidate's time is the least wall time of `repeats`
+ * (1..100) encodes after one untimed encode. Every candidate must reproduce
+ * the first encode's codestreams byte for byte; a difference, or a failed
+ * encode, restores the previous options and returns JP2G_ENCODE_FAILED.
+ * `best` (JP2G_NUM_OPTS entries) and `best_ms` may be NULL. No reference
+ * counterpart: the reference has no tunable device schedule. */
+int jp2g_autotune(jp2g_ctx* ctx, const jp2g_request* reqs, uint32_t n, int repeats, int64_t* best,
+                  double* best_ms);
 
 /* Message of the last failed call on this context (or of the last failed
  * jp2g_create when ctx is NULL). */

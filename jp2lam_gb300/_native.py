@@ -51,6 +51,7 @@ EXPORTS = [
     "jp2g_last_error", "jp2g_stream", "jp2g_set_timing", "jp2g_stage_times", "jp2g_counters",
     "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
     "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
+    "jp2g_autotune",
 ]
 
 PENDING = 6
@@ -60,6 +61,7 @@ OPT_HOST_THREADS = 2
 OPT_MQ_WARPS_PER_SM = 3
 OPT_MQ_PIPES_PER_SM = 4
 OPT_MQ_HEAVY = 5
+NUM_OPTS = 6
 
 
 class Request(ctypes.Structure):
@@ -116,6 +118,8 @@ def load_library(path: str = LIB_PATH):
                                   ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]
         lib.jp2g_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
         lib.jp2g_get_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+        lib.jp2g_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_uint32, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)]
         _lib = lib
         return lib
 
@@ -255,6 +259,22 @@ class Engine:
         v = ctypes.c_int64()
         self._check(self.lib.jp2g_get_option(self.handle, option, ctypes.byref(v)))
         return v.value
+
+    def autotune(self, pages, repeats: int = 2):
+        """Picks the fastest MQ schedule and wave size for a sample of page
+        dicts (as encode_batch takes them) and leaves it set; returns
+        ({option: value}, wall ms of one encode of the sample)."""
+        keep = []
+        n = len(pages)
+        reqs = (Request * max(n, 1))(*[self._request(p, keep) for p in pages])
+        best = (ctypes.c_int64 * NUM_OPTS)()
+        ms = ctypes.c_double()
+        with self._lock:
+            rc = self.lib.jp2g_autotune(self.handle, reqs, n, repeats, best, ctypes.byref(ms))
+            msg = self.lib.jp2g_last_error(self.handle).decode() if rc != 0 else ""
+        if rc != 0:
+            raise _BY_CODE.get(rc, Jp2LamError)(msg)
+        return {i: best[i] for i in range(NUM_OPTS)}, ms.value
 
     def stream(self) -> int:
         return self.lib.jp2g_stream(self.handle)

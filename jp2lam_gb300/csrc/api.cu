@@ -818,8 +818,14 @@ int encode_one(jp2g_ctx* c, PageJob* j, WaveDebug* dbg) {
 // wave of its own) and at most kMaxWavePages pages (band constants are
 // indexed by 16 bits, 19 per page at most).
 constexpr size_t kMaxWavePages = 3000;
+// Code-blocks one wave may hold: the wave-size option, capped so that the
+// wave's payload slots stay addressable with 32-bit byte offsets.
+uint64_t wave_block_limit(const jp2g_ctx* c, int cbw) {
+  const uint64_t cap = (uint64_t)cbw * (uint64_t)cbw * 4u + 1024u;  // slot_cap of a cbw x cbw block
+  return std::min<uint64_t>((uint64_t)c->opt[JP2G_OPT_WAVE_BLOCKS], 0xffffffffull / cap);
+}
+
 std::vector<std::vector<PageJob*>> form_waves(jp2g_ctx* c, const std::vector<PageJob*>& jobs) {
-  const uint64_t limit = c->opt[JP2G_OPT_WAVE_BLOCKS];
   std::vector<std::vector<PageJob*>> waves;
   std::vector<PageJob*> cur;
   uint64_t cur_blocks = 0;
@@ -833,7 +839,8 @@ std::vector<std::vector<PageJob*>> form_waves(jp2g_ctx* c, const std::vector<Pag
       nb = p.nblocks;
       cbw = p.cbw;
     }
-    if (!cur.empty() && (cbw != cur_cbw || cur_blocks + nb > limit || cur.size() >= kMaxWavePages)) {
+    if (!cur.empty() &&
+        (cbw != cur_cbw || cur_blocks + nb > wave_block_limit(c, cbw) || cur.size() >= kMaxWavePages)) {
       waves.push_back(std::move(cur));
       cur.clear();
       cur_blocks = 0;
@@ -1077,7 +1084,7 @@ void worker_loop(jp2g_ctx* c) {
       int cbw = 0;
       while (!c->pending.empty() && wave.size() < kMaxWavePages) {
         const PagePlan& p = c->pending.front()->job.plan;
-        if (!wave.empty() && (p.cbw != cbw || blocks + p.nblocks > (uint64_t)c->opt[JP2G_OPT_WAVE_BLOCKS]))
+        if (!wave.empty() && (p.cbw != cbw || blocks + p.nblocks > wave_block_limit(c, p.cbw)))
           break;
         cbw = p.cbw;
         blocks += p.nblocks;
@@ -1210,6 +1217,109 @@ int jp2g_get_option(jp2g_ctx* c, int option, int64_t* value) {
   if (!c || !value || option < 0 || option >= JP2G_NUM_OPTS) return JP2G_INVALID_INPUT;
   std::lock_guard<std::mutex> lk(c->mu);
   *value = c->opt[option];
+  return JP2G_OK;
+}
+
+// Two stages over the scheduling knobs: the MQ schedule at the context's
+// wave size, then the wave size under the chosen schedule. A candidate is
+// timed as the minimum wall time of `repeats` encodes of the sample after
+// one untimed encode, and must reproduce the first encode's codestreams.
+int jp2g_autotune(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, int repeats, int64_t* best,
+                  double* best_ms) {
+  if (!c) return JP2G_INVALID_INPUT;
+  if (n == 0 || !reqs || repeats < 1 || repeats > 100)
+    return set_err(c, JP2G_INVALID_INPUT, "autotune needs at least one sample page and 1..100 repeats");
+  int64_t saved[JP2G_NUM_OPTS];
+  for (int i = 0; i < JP2G_NUM_OPTS; ++i) jp2g_get_option(c, i, &saved[i]);
+  auto restore = [&] {
+    for (int i = 0; i < JP2G_NUM_OPTS; ++i) jp2g_set_option(c, i, saved[i]);
+  };
+  std::vector<uint8_t*> outs(n);
+  std::vector<size_t> lens(n);
+  std::vector<int> st(n), ref_st(n);
+  std::vector<std::string> ref(n);
+  // One encode of the sample under `o`: its wall time in ms, -1 if the call
+  // failed, -2 if a codestream differs from the reference encode.
+  auto encode_once = [&](const int64_t* o, bool record) -> double {
+    for (int i = 0; i < JP2G_NUM_OPTS; ++i)
+      if (jp2g_set_option(c, i, o[i]) != JP2G_OK) return -1.0;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = jp2g_encode_batch(c, reqs, n, outs.data(), lens.data(), st.data());
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    bool same = true;
+    for (uint32_t i = 0; i < n; ++i) {
+      std::string bytes = outs[i] ? std::string(reinterpret_cast<const char*>(outs[i]), lens[i]) : std::string();
+      if (record) {
+        ref[i] = std::move(bytes);
+        ref_st[i] = st[i];
+      } else if (st[i] != ref_st[i] || bytes != ref[i]) {
+        same = false;
+      }
+      jp2g_free(outs[i]);
+      outs[i] = nullptr;
+    }
+    if (rc != JP2G_OK) return -1.0;
+    return same ? ms : -2.0;
+  };
+  auto time_candidate = [&](const int64_t* o) -> double {
+    double t = encode_once(o, false);  // untimed: settles buffers for this setting
+    if (t < 0) return t;
+    double m = 1e300;
+    for (int r = 0; r < repeats; ++r) {
+      t = encode_once(o, false);
+      if (t < 0) return t;
+      m = std::min(m, t);
+    }
+    return m;
+  };
+  auto fail = [&](const int64_t* o, double why) {
+    restore();
+    if (why == -2.0)
+      return set_err(c, JP2G_ENCODE_FAILED,
+                     "autotune: a scheduling setting changed the codestream (mq_blocks_per_warp=" +
+                         std::to_string(o[JP2G_OPT_MQ_BLOCKS_PER_WARP]) + ", mq_warps_per_sm=" +
+                         std::to_string(o[JP2G_OPT_MQ_WARPS_PER_SM]) + ", mq_pipes_per_sm=" +
+                         std::to_string(o[JP2G_OPT_MQ_PIPES_PER_SM]) + ", wave_blocks=" +
+                         std::to_string(o[JP2G_OPT_WAVE_BLOCKS]) + ")");
+    return set_err(c, JP2G_ENCODE_FAILED, "autotune: the sample failed to encode: " + get_msg(c));
+  };
+  if (encode_once(saved, true) < 0) return fail(saved, -1.0);
+
+  // stage 1: MQ schedule (automatic; producer/consumer pipelines; single-warp
+  // pulling; blocks packed per warp)
+  struct Mq { int64_t bpw, wps, pipes; };
+  const Mq mq[] = {{0, 0, 0},  {1, 0, 4},  {1, 0, 8},  {1, 0, 16}, {1, 8, -1}, {1, 12, -1},
+                   {1, 16, -1}, {2, 0, 0}, {4, 0, 0},  {8, 0, 0},  {16, 0, 0}, {32, 0, 0}};
+  int64_t cur[JP2G_NUM_OPTS], win[JP2G_NUM_OPTS];
+  std::memcpy(cur, saved, sizeof cur);
+  cur[JP2G_OPT_MQ_HEAVY] = 0;
+  double win_ms = 1e300;
+  for (const Mq& m : mq) {
+    cur[JP2G_OPT_MQ_BLOCKS_PER_WARP] = m.bpw;
+    cur[JP2G_OPT_MQ_WARPS_PER_SM] = m.wps;
+    cur[JP2G_OPT_MQ_PIPES_PER_SM] = m.pipes;
+    const double t = time_candidate(cur);
+    if (t < 0) return fail(cur, t);
+    if (t < win_ms) {
+      win_ms = t;
+      std::memcpy(win, cur, sizeof win);
+    }
+  }
+  // stage 2: device wave size under the chosen schedule
+  std::memcpy(cur, win, sizeof cur);
+  for (int64_t wb : {20000ll, 40000ll, 80000ll, 160000ll, 240000ll}) {
+    if (wb == win[JP2G_OPT_WAVE_BLOCKS]) continue;
+    cur[JP2G_OPT_WAVE_BLOCKS] = wb;
+    const double t = time_candidate(cur);
+    if (t < 0) return fail(cur, t);
+    if (t < win_ms) {
+      win_ms = t;
+      win[JP2G_OPT_WAVE_BLOCKS] = wb;
+    }
+  }
+  for (int i = 0; i < JP2G_NUM_OPTS; ++i) jp2g_set_option(c, i, win[i]);
+  if (best) std::memcpy(best, win, sizeof win);
+  if (best_ms) *best_ms = win_ms;
   return JP2G_OK;
 }
 

@@ -192,3 +192,44 @@ def test_mq_schedules_do_not_change_output(eng, orc, wps, pipes, heavy, q):
     finally:
         for o, v in zip(opts, old):
             eng.set_option(o, v)
+
+
+def test_autotune_keeps_output_and_leaves_its_choice_set(eng):
+    pages = _mix(8, 8, big=True)
+    ref = eng.encode_batch(pages)
+    opts = list(range(_native.NUM_OPTS))
+    old = [eng.get_option(o) for o in opts]
+    try:
+        best, ms = eng.autotune(pages, repeats=1)
+        assert ms > 0
+        assert [eng.get_option(o) for o in opts] == [best[o] for o in opts]
+        assert 0 <= best[_native.OPT_MQ_BLOCKS_PER_WARP] <= 32
+        assert best[_native.OPT_WAVE_BLOCKS] in (old[0], 20000, 40000, 80000, 160000, 320000)
+        assert best[_native.OPT_HOST_THREADS] == old[_native.OPT_HOST_THREADS]
+        assert eng.encode_batch(pages) == ref
+    finally:
+        for o, v in zip(opts, old):
+            eng.set_option(o, v)
+
+
+def test_autotune_rejects_an_empty_sample(eng):
+    with pytest.raises(jl.InvalidInput):
+        eng.autotune([], repeats=1)
+    with pytest.raises(jl.InvalidInput):
+        eng.autotune(_mix(1, 9), repeats=0)
+
+
+def test_wave_size_is_capped_to_addressable_payload_slots(eng):
+    # 40 sRGB 2550x3300 pages hold 252,840 64x64 code-blocks: more than one
+    # wave can address, so a larger wave-size option still splits them
+    pages = [{"px": synth_page(2550, 3300, 3, 1000 + i, photo_w=800, photo_h=600), "w": 2550, "h": 3300,
+              "ncomp": 3, "quality": 75, "fmt": 1} for i in range(40)]
+    ref = eng.encode_batch(pages[:2])
+    old = eng.get_option(_native.OPT_WAVE_BLOCKS)
+    try:
+        eng.set_option(_native.OPT_WAVE_BLOCKS, 10 ** 9)
+        outs = eng.encode_batch(pages)
+    finally:
+        eng.set_option(_native.OPT_WAVE_BLOCKS, old)
+    assert all(isinstance(o, bytes) for o in outs)
+    assert outs[:2] == ref
