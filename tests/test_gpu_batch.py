@@ -204,7 +204,7 @@ def test_autotune_keeps_output_and_leaves_its_choice_set(eng):
         assert ms > 0
         assert [eng.get_option(o) for o in opts] == [best[o] for o in opts]
         assert 0 <= best[_native.OPT_MQ_BLOCKS_PER_WARP] <= 32
-        assert best[_native.OPT_WAVE_BLOCKS] in (old[0], 20000, 40000, 80000, 160000, 320000)
+        assert best[_native.OPT_WAVE_BLOCKS] in (old[0], 20000, 40000, 80000, 160000, 240000)
         assert best[_native.OPT_HOST_THREADS] == old[_native.OPT_HOST_THREADS]
         assert eng.encode_batch(pages) == ref
     finally:
