@@ -65,6 +65,7 @@ struct PageJob {
   PagePlan plan;            // band first_block relative to the page
   uint32_t block_base = 0;  // the page's first code-block in the wave
   size_t px_off = 0;        // the page's pixels in the wave's staging buffer
+  bool staged = false;      // copied to the device from pinned staging
   std::vector<BlockKeep> keep;
   std::vector<uint32_t> offsets;  // nblocks + 1 body offsets
   std::vector<uint8_t> body;
@@ -441,23 +442,38 @@ constexpr size_t kStageFailed = ~size_t(0);
 // tasks over the host threads.
 // Planar RGB must be interleaved on the way; pages above 32 MiB are copied
 // faster by the host threads into pinned memory than by one pageable copy.
+// Host pixels reach the device one copy per page. A wave holding at most
+// kDirectCopyMax bytes of host pixels copies pages in the device layout
+// straight from the caller's memory; a larger wave (a big page, or many
+// pages) is first gathered into pinned staging by the host threads, so its
+// copies run at the link's pinned rate, and for every wave after a batch's
+// first the gathering overlaps the previous wave's device work. Planar RGB
+// is always staged: it is interleaved on the way.
 constexpr size_t kDirectCopyMax = 32u << 20;
-bool needs_staging(const PageJob* j) {
-  return (j->ncomp == 3 && !j->interleaved) || (size_t)j->w * j->h * j->ncomp > kDirectCopyMax;
+bool needs_staging(const PageJob* j, size_t wave_host_bytes) {
+  return (j->ncomp == 3 && !j->interleaved) || wave_host_bytes > kDirectCopyMax;
 }
 
 size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
-  size_t total = 0;
-  std::vector<PageJob*> staged;
+  size_t total = 0, host_bytes = 0;
+  std::vector<PageJob*> paged;
   for (size_t i = 0; i < n; ++i) {
     PageJob* j = jobs[i];
     PagePlan p;
     Failure f{};
+    j->staged = false;
     if (!j->host_px || !build_plan(j->w, j->h, (int)j->ncomp, j->quality, j->format, &p, &f)) continue;
     j->px_off = total;
     total += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
-    if (needs_staging(j)) staged.push_back(j);
+    host_bytes += (size_t)j->w * j->h * j->ncomp;
+    paged.push_back(j);
   }
+  std::vector<PageJob*> staged;
+  for (PageJob* j : paged)
+    if (needs_staging(j, host_bytes)) {
+      j->staged = true;
+      staged.push_back(j);
+    }
   if (staged.empty()) return total;
   if (!reserve_host(c, buf, total)) return kStageFailed;
   uint8_t* staging = reinterpret_cast<uint8_t*>(buf.p);
@@ -583,7 +599,7 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
     // memory for small pages in the device layout
     for (PageJob* j : live) {
       if (!j->host_px) continue;
-      const uint8_t* from = needs_staging(j) ? staging + j->px_off : j->host_px;
+      const uint8_t* from = j->staged ? staging + j->px_off : j->host_px;
       if (!cuda_ok(c, cudaMemcpyAsync(dptr<uint8_t>(c->px) + j->px_off, from, (size_t)j->w * j->h * j->ncomp,
                                       cudaMemcpyHostToDevice, c->stream), "H2D"))
         return kEncodeFailed;
