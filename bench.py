@@ -488,18 +488,22 @@ def main():
     dwt_gbs = gbs("dwt")
     dominant = max(kernels, key=lambda k: kernels[k][2])
     traffic = None
+    issue = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
         traffic = prof.get(kernels[dominant][0].split(" ")[0])
+        issue = prof.get("_issue_active", {}).get(kernels[dominant][0].split(" ")[0])
     except Exception:
         pass
     roof = {"kernel": kernels[dominant][0], "bound": "hbm", "achieved": gbs(dominant), "peak": hbm,
             "unit": "GB/s", "frac": gbs(dominant) / hbm if gbs(dominant) else None, "traffic": traffic,
             "algorithmic_bytes_per_launch": kernels[dominant][1], "launch_ms": kernels[dominant][2]}
     if dominant == "t1_mq":
-        roof["note"] = ("MQ coding is a serial chain per code-block, so a single page is bound by the "
-                        "heaviest block's chain latency, not by HBM; the fraction shows the distance "
-                        "to the bandwidth roof")
+        roof["note"] = ("MQ coding is a serial chain per code-block: a single page is bound by "
+                        "instruction issue (issue_active, from the committed ncu capture) and the "
+                        "heaviest block's chain, not by HBM; the fraction shows the distance to the "
+                        "bandwidth roof")
+        roof["issue_active"] = issue
         roof["mq_symbols_per_s"] = counters[7] / (st_mean["t1_mq"] / 1e3) if st_mean["t1_mq"] else None
     roof["peak_source"] = "measured" if "fallback" not in peaks else "fallback"
 
