@@ -199,7 +199,7 @@ def _time_calls(fn, steps, warmup, stream, torch):
 
 
 OPT_NAMES = ["wave_blocks", "mq_blocks_per_warp", "host_threads", "mq_warps_per_sm", "mq_pipes_per_sm",
-             "mq_heavy"]
+             "mq_heavy", "mq_chains_per_pair"]
 
 
 def _autotune(eng, dpages, args):

@@ -112,7 +112,7 @@ int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, in
  *                             838,860 32x32 blocks, whose payload slots need
  *                             32-bit offsets);
  * JP2G_OPT_MQ_BLOCKS_PER_WARP code-blocks per warp in MQ coding, 1..32, or 0
- *                             for automatic (1 up to 16 blocks per SM, else
+ *                             for automatic (1 up to 48 blocks per SM, else
  *                             2..32 for about 24 warps per SM);
  * JP2G_OPT_HOST_THREADS       host threads for staging and Tier-2 (0 = all but
  *                             two hardware threads);
@@ -123,12 +123,16 @@ int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, in
  * JP2G_OPT_MQ_PIPES_PER_SM    when pulling: producer/consumer warp pairs per
  *                             SM that split each block's MQ chain into its
  *                             interval and code-register halves (0 =
- *                             automatic: 8 pairs up to 16 blocks per SM,
- *                             single-warp pulling above; -1 = single-warp
- *                             pulling);
+ *                             automatic: 8 pairs per SM up to 48 blocks per
+ *                             SM; -1 = single-warp pulling);
  * JP2G_OPT_MQ_HEAVY           with pipelines: how many of the heaviest blocks
  *                             they take, the rest being coded 32 to a warp
- *                             (0 = all blocks). */
+ *                             (0 = all blocks);
+ * JP2G_OPT_MQ_CHAINS_PER_PAIR with pipelines: code-blocks each pair codes at
+ *                             once, 1 (all lanes of a warp on one chain) or 2
+ *                             (one per half-warp: about half the issue slots
+ *                             per symbol); 0 = automatic (1 up to 8 blocks
+ *                             per SM, else 2). */
 enum {
   JP2G_OPT_WAVE_BLOCKS = 0,
   JP2G_OPT_MQ_BLOCKS_PER_WARP = 1,
@@ -136,15 +140,16 @@ enum {
   JP2G_OPT_MQ_WARPS_PER_SM = 3,
   JP2G_OPT_MQ_PIPES_PER_SM = 4,
   JP2G_OPT_MQ_HEAVY = 5,
-  JP2G_NUM_OPTS = 6
+  JP2G_OPT_MQ_CHAINS_PER_PAIR = 6,
+  JP2G_NUM_OPTS = 7
 };
 int jp2g_set_option(jp2g_ctx* ctx, int option, int64_t value);
 int jp2g_get_option(jp2g_ctx* ctx, int option, int64_t* value);
 
 /* Autotuner: encodes the caller's sample pages (through jp2g_encode_batch)
  * under each candidate setting of the MQ schedule (automatic; 4, 8 or 16
- * producer/consumer pairs per SM; 8, 12 or 16 pulling warps per SM; 2 to 32
- * blocks packed per warp), then of the wave size (20,000 to 240,000
+ * producer/consumer pairs per SM with one or two chains each; 8, 12 or 16
+ * pulling warps per SM; 2 to 32 blocks packed per warp), then of the wave size (20,000 to 240,000
  * code-blocks) under the fastest schedule, and leaves the fastest setting on
  * the context. A candidate's time is the least wall time of `repeats`
  * (1..100) encodes after one untimed encode. Every candidate must reproduce

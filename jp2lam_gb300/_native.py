@@ -61,7 +61,8 @@ OPT_HOST_THREADS = 2
 OPT_MQ_WARPS_PER_SM = 3
 OPT_MQ_PIPES_PER_SM = 4
 OPT_MQ_HEAVY = 5
-NUM_OPTS = 6
+OPT_MQ_CHAINS_PER_PAIR = 6
+NUM_OPTS = 7
 
 
 class Request(ctypes.Structure):

@@ -100,7 +100,7 @@ struct jp2g_ctx {
   cudaEvent_t ev[kNumEvents] = {};
   float stage_ms[kNumStages + 3] = {};
   uint64_t counters[8] = {};
-  int64_t opt[JP2G_NUM_OPTS] = {160000, 0, 0, 0, 0, 0};
+  int64_t opt[JP2G_NUM_OPTS] = {160000, 0, 0, 0, 0, 0, 0};
   // submit/poll: a worker thread forms waves from the queue and runs their
   // device phase; a finisher thread runs Tier-2 of finished waves, so the
   // next wave's device work overlaps the previous wave's host work.
@@ -394,6 +394,17 @@ int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live) {
   return kOk;
 }
 
+// Code-blocks each MQ producer/consumer pair codes at once. Automatic: one
+// (all lanes on the chain) up to 8 blocks per SM, where the heaviest
+// block's chain sets the time; two (one per half-warp) above, where
+// instruction issue does (measured on 1700x2200 to 3400x4400 gray pages and
+// a 2550x3300 sRGB page).
+int mq_chains_per_pair(const jp2g_ctx* c, uint32_t nb) {
+  const int64_t v = c->opt[JP2G_OPT_MQ_CHAINS_PER_PAIR];
+  if (v == 1 || v == 2) return (int)v;
+  return nb > (uint32_t)c->num_sms * 8u ? 2 : 1;
+}
+
 // Runs f(0..n-1) on up to `threads` host threads.
 template <class F>
 void parallel_for(size_t n, int threads, F f) {
@@ -659,9 +670,9 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
   // warp's lanes carry similar symbol counts; with one block per warp by a
   // fixed number of warps per SM that pull blocks in that order, so the
   // longest chains start first and share their schedulers with few others.
-  // Automatic choice (measured on 1275x1650 to 3400x4400 pages): up to 16
-  // blocks per SM, producer/consumer pipelines pulling one block each;
-  // beyond that, 2..32 blocks packed per warp.
+  // Automatic choice (measured on 1275x1650 to 5100x6600 pages): up to 48
+  // blocks per SM, producer/consumer pipelines pulling blocks; beyond that,
+  // 2..32 blocks packed per warp.
   const int64_t bpw_opt = c->opt[JP2G_OPT_MQ_BLOCKS_PER_WARP];
   const int64_t wps_opt = c->opt[JP2G_OPT_MQ_WARPS_PER_SM];
   const uint32_t sms = (uint32_t)c->num_sms;
@@ -676,14 +687,14 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
     ta.mq_order = dptr<uint32_t>(c->mqorder);
     order_launches = 3;
   }
-  // Producer/consumer pairs shorten each block's chain; they pay off while
-  // one heavy chain sets the time (up to 16 blocks per SM, 8 pairs per SM);
-  // beyond that single-warp pulling keeps more chains in flight.
+  // Producer/consumer pairs shorten each block's chain (8 pairs per SM, one
+  // or two chains each); up to 48 blocks per SM they beat single-warp
+  // pulling and packed warps.
   const int64_t pipes_opt = c->opt[JP2G_OPT_MQ_PIPES_PER_SM];
-  const bool use_pipe = use_pull && (pipes_opt > 0 || (pipes_opt == 0 && nb <= sms * 16u));
+  const bool use_pipe = use_pull && (pipes_opt > 0 || (pipes_opt == 0 && nb <= sms * 48u));
   if (use_pipe)
-    launch_t1_mq_pipe(ta, c->num_sms, pipes_opt > 0 ? (int)pipes_opt : 8, (uint32_t)c->opt[JP2G_OPT_MQ_HEAVY],
-                      dptr<uint32_t>(c->stats) + 2, c->stream);
+    launch_t1_mq_pipe(ta, c->num_sms, pipes_opt > 0 ? (int)pipes_opt : 8, mq_chains_per_pair(c, nb),
+                      (uint32_t)c->opt[JP2G_OPT_MQ_HEAVY], dptr<uint32_t>(c->stats) + 2, c->stream);
   else if (use_pull)
     launch_t1_mq_pull(ta, c->num_sms, pull, dptr<uint32_t>(c->stats) + 2, c->stream);
   else
@@ -1222,6 +1233,9 @@ int jp2g_set_option(jp2g_ctx* c, int option, int64_t value) {
     case JP2G_OPT_MQ_HEAVY:
       if (value < 0 || value > 0xffffffffll) return set_err(c, JP2G_INVALID_INPUT, "mq_heavy must be >= 0");
       break;
+    case JP2G_OPT_MQ_CHAINS_PER_PAIR:
+      if (value < 0 || value > 2) return set_err(c, JP2G_INVALID_INPUT, "mq_chains_per_pair must be 0..2");
+      break;
     default:
       return set_err(c, JP2G_INVALID_INPUT, "unknown option " + std::to_string(option));
   }
@@ -1303,9 +1317,10 @@ int jp2g_autotune(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, int repeats
 
   // stage 1: MQ schedule (automatic; producer/consumer pipelines; single-warp
   // pulling; blocks packed per warp)
-  struct Mq { int64_t bpw, wps, pipes; };
-  const Mq mq[] = {{0, 0, 0},  {1, 0, 4},  {1, 0, 8},  {1, 0, 16}, {1, 8, -1}, {1, 12, -1},
-                   {1, 16, -1}, {2, 0, 0}, {4, 0, 0},  {8, 0, 0},  {16, 0, 0}, {32, 0, 0}};
+  struct Mq { int64_t bpw, wps, pipes, chains; };
+  const Mq mq[] = {{0, 0, 0, 0},   {1, 0, 4, 1},   {1, 0, 8, 1},   {1, 0, 16, 1}, {1, 0, 4, 2},
+                   {1, 0, 8, 2},   {1, 0, 16, 2},  {1, 8, -1, 0},  {1, 12, -1, 0}, {1, 16, -1, 0},
+                   {2, 0, 0, 0},   {4, 0, 0, 0},   {8, 0, 0, 0},   {16, 0, 0, 0}, {32, 0, 0, 0}};
   int64_t cur[JP2G_NUM_OPTS], win[JP2G_NUM_OPTS];
   std::memcpy(cur, saved, sizeof cur);
   cur[JP2G_OPT_MQ_HEAVY] = 0;
@@ -1314,6 +1329,7 @@ int jp2g_autotune(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, int repeats
     cur[JP2G_OPT_MQ_BLOCKS_PER_WARP] = m.bpw;
     cur[JP2G_OPT_MQ_WARPS_PER_SM] = m.wps;
     cur[JP2G_OPT_MQ_PIPES_PER_SM] = m.pipes;
+    cur[JP2G_OPT_MQ_CHAINS_PER_PAIR] = m.chains;
     const double t = time_candidate(cur);
     if (t < 0) return fail(cur, t);
     if (t < win_ms) {

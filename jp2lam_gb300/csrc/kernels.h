@@ -74,12 +74,13 @@ void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st);
 // One block per warp, blocks taken in a.mq_order from an atomic counter
 // (*next, zeroed here) by warps_per_sm warps on each SM.
 void launch_t1_mq_pull(const T1Args& a, int num_sms, int warps_per_sm, uint32_t* next, cudaStream_t st);
-// One block per producer/consumer warp pair (interval chain | code register
-// chain), pairs pulling the `heavy` first blocks of a.mq_order (0 = all)
-// from *next (zeroed here), pipes_per_sm pairs on each SM; the remaining
-// blocks are coded 32 to a warp in the same launch.
-void launch_t1_mq_pipe(const T1Args& a, int num_sms, int pipes_per_sm, uint32_t heavy, uint32_t* next,
-                       cudaStream_t st);
+// Producer/consumer warp pairs (interval chain | code register chain)
+// coding `chains` blocks at once each (1: all lanes of a warp on one chain;
+// 2: one chain per half-warp), pulling the `heavy` first blocks of
+// a.mq_order (0 = all) from *next (zeroed here), pipes_per_sm pairs on each
+// SM; the remaining blocks are coded 32 to a warp in the same launch.
+void launch_t1_mq_pipe(const T1Args& a, int num_sms, int pipes_per_sm, int chains, uint32_t heavy,
+                       uint32_t* next, cudaStream_t st);
 // Code-blocks per warp that launch_t1_mq uses for `bpw` (0 = automatic).
 int mq_blocks_per_warp(const T1Args& a, int num_sms, int bpw);
 // Orders the blocks by their MQ symbol count, largest first (counting sort

@@ -718,8 +718,13 @@ struct PipeChunk {
   uint32_t op[16];
 };
 
+// Barrier `id` of one producer/consumer pair (64 threads). With two chains
+// per warp the halves of a warp may arrive apart, so that form uses the
+// barrier that does not require a converged warp.
+template <int H>
 __device__ __forceinline__ void pipe_bar(int id) {
-  asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory");
+  if constexpr (H == 1) asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory");
+  else asm volatile("barrier.sync %0, 64;" ::"r"(id) : "memory");
 }
 
 // State entry with its successors: x = qe | leading zeros of qe << 16 |
@@ -814,11 +819,20 @@ __device__ __forceinline__ void phase_c_one(Mq& m, uint32_t op) {
 // CTAs below pipe_ctas are pipelines that pull the `heavy` heaviest blocks;
 // the CTAs above code the remaining (lighter) blocks 32 to a warp, one per
 // lane, which costs the schedulers far fewer issue slots per symbol.
+//
+// H chains per warp pair: with H = 2 the two half-warps of each warp run the
+// chains of two different code-blocks in the same instruction stream (each
+// half pulls its own blocks), so a symbol costs about half the issue slots
+// of H = 1 (all 32 lanes on one chain), at the price of executing both
+// halves' byte-output branches. A half with nothing left keeps taking part
+// in the pair's barriers with empty chunks until both halves are done.
+template <int H>
 __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, uint32_t* next, uint32_t pipe_ctas,
                                                                 uint32_t heavy) {
+  constexpr int HL = 32 / H;  // lanes per chain
   __shared__ uint4 F[94];
-  __shared__ PipeChunk slots[kPipes][2];
-  __shared__ uint32_t ci_all[kPipes][20];
+  __shared__ PipeChunk slots[kPipes][2][H];
+  __shared__ uint32_t ci_all[kPipes][H][20];
   if (blockIdx.x >= pipe_ctas) {
     __shared__ uint2 T[94];
     __shared__ uint2 ce_all[kPipes * 2][20 * 32];
@@ -832,16 +846,18 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
   load_fat_table(F);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int half = lane / HL, hl = lane % HL;  // this lane's chain, its lane within it
+  const uint32_t hmask = H == 1 ? 0xffffffffu : (0xffffu << (16 * half));
   // producers are warps 0..kPipes-1 and consumers the warps above, so the
   // (heavier) producer chains spread over the SM's schedulers
   const int pipe = warp % kPipes;
   const int bar = 1 + pipe;
-  PipeChunk* slot = slots[pipe];
   if (warp < kPipes) {
     // ---- producer: interval and state chain ----
-    uint32_t* ci = ci_all[pipe];
+    uint32_t* ci = ci_all[pipe][half];
     uint32_t b = kPipeEnd, base = 0, A = 0x8000u;
     int mbp = 0, j = 0, lo = 0, total = 0;
+    bool exhausted = false;  // the block queue is empty for this chain
     const uint4* src = nullptr;
     uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0, c2 = c0;
     auto start_item = [&]() {
@@ -854,13 +870,16 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
       c2 = src[2];  // the slot and the buffer are padded for these reads
     };
     for (uint32_t k = 0;; ++k) {
-      PipeChunk& s = slot[k & 1];
+      PipeChunk& s = slots[pipe][k & 1][half];
       uint32_t flags = 0;
-      while (b == kPipeEnd) {
+      while (b == kPipeEnd && !exhausted) {
         uint32_t t = 0;
-        if (lane == 0) t = atomicAdd(next, 1u);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= heavy) break;
+        if (hl == 0) t = atomicAdd(next, 1u);
+        t = __shfl_sync(hmask, t, half * HL);
+        if (t >= heavy) {
+          exhausted = true;
+          break;
+        }
         const uint32_t cand = a.mq_order[t];
         const BlockOut o = a.res[cand];
         const int m_ = o.status ? 0 : o.mbp;
@@ -871,56 +890,56 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
         base = a.plane_base[b];
         A = 0x8000u;
         // contexts: state 0 except UNI 46, AGG 3, ZC 4 (src/mq/mod.rs:195-200)
-        if (lane < 19) ci[lane] = lane == kCtxUNI ? 92u : (lane == kCtxAGG ? 6u : (lane == 0 ? 8u : 0u));
-        __syncwarp();
+        for (int x = hl; x < 19; x += HL) ci[x] = x == kCtxUNI ? 92u : (x == kCtxAGG ? 6u : (x == 0 ? 8u : 0u));
+        __syncwarp(hmask);
         flags = 1;
         start_item();
       }
-      if (b == kPipeEnd) {
-        if (lane == 0) s.block = kPipeEnd;
-        __syncwarp();
-        pipe_bar(bar);
-        break;
-      }
-      const int cnt = min(16, total - lo);
-      if (cnt == 16) {
-        const uint4 q = c0;
-        c0 = c1;
-        c1 = c2;
-        c2 = src[(lo >> 4) + 3];  // 48 bytes ahead: inside the slot or the buffer's pad
-        uint32_t op[16];
-        phase_a_chunk(A, ci, F, q, op);
-        if (lane == 0) {
-          #pragma unroll
-          for (int i = 0; i < 16; ++i) s.op[i] = op[i];
-        }
+      const bool idle = b == kPipeEnd;
+      if (idle) {
+        if (hl == 0) s.block = kPipeEnd;
       } else {
-        const uint4 q = c0;
-        for (int i = 0; i < cnt; ++i) {
-          const uint32_t o = phase_a_one(A, ci, F, chunk_sym(q, i));
-          if (lane == 0) s.op[i] = o;
-        }
-      }
-      if (lane == 0) {
-        s.block = b;
-        s.item = (uint16_t)j;
-        s.lo = (uint16_t)lo;
-        s.count = (uint32_t)cnt;
-      }
-      lo += cnt;
-      if (lo >= total) {
-        flags |= 2;
-        if (++j == mbp) {
-          flags |= 4;
-          if (lane == 0) s.a_end = A;
-          b = kPipeEnd;
+        const int cnt = min(16, total - lo);
+        if (cnt == 16) {
+          const uint4 q = c0;
+          c0 = c1;
+          c1 = c2;
+          c2 = src[(lo >> 4) + 3];  // 48 bytes ahead: inside the slot or the buffer's pad
+          uint32_t op[16];
+          phase_a_chunk(A, ci, F, q, op);
+          if (hl == 0) {
+            #pragma unroll
+            for (int i = 0; i < 16; ++i) s.op[i] = op[i];
+          }
         } else {
-          start_item();
+          const uint4 q = c0;
+          for (int i = 0; i < cnt; ++i) {
+            const uint32_t o = phase_a_one(A, ci, F, chunk_sym(q, i));
+            if (hl == 0) s.op[i] = o;
+          }
         }
+        if (hl == 0) {
+          s.block = b;
+          s.item = (uint16_t)j;
+          s.lo = (uint16_t)lo;
+          s.count = (uint32_t)cnt;
+        }
+        lo += cnt;
+        if (lo >= total) {
+          flags |= 2;
+          if (++j == mbp) {
+            flags |= 4;
+            if (hl == 0) s.a_end = A;
+            b = kPipeEnd;
+          } else {
+            start_item();
+          }
+        }
+        if (hl == 0) s.flags = flags;
       }
-      if (lane == 0) s.flags = flags;
-      __syncwarp();
-      pipe_bar(bar);
+      const bool all_idle = __all_sync(0xffffffffu, idle);
+      pipe_bar<H>(bar);
+      if (all_idle) break;
     }
   } else {
     // ---- consumer: code register chain, bytes and pass records ----
@@ -942,10 +961,12 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
       ++pi;
     };
     for (uint32_t k = 0;; ++k) {
-      pipe_bar(bar);
-      const PipeChunk& s = slot[k & 1];
+      __syncwarp();  // the halves meet before the pair's barrier
+      pipe_bar<H>(bar);
+      const PipeChunk& s = slots[pipe][k & 1][half];
       const uint32_t blk = s.block;
-      if (blk == kPipeEnd) break;
+      if (__all_sync(0xffffffffu, blk == kPipeEnd)) break;
+      if (blk == kPipeEnd) continue;  // this chain is idle in this round
       const uint32_t flags = s.flags;
       const int item = s.item, lo = s.lo, cnt = (int)s.count;
       if (flags & 1) {
@@ -988,7 +1009,7 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
         mq_flush(m);
         o.payload_len = (uint32_t)(m.last == 0xffu ? m.pos - 1 : m.pos);  // take_bytes
         o.status = m.ovf ? 1 : 0;
-        if (lane == 0) {
+        if (hl == 0) {
           a.res[blk] = o;
           atomicAdd(a.sym_count, (unsigned long long)nsym);
         }
@@ -1060,13 +1081,13 @@ void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st) {
 }
 
 int mq_blocks_per_warp(const T1Args& a, int num_sms, int bpw) {
-  // Automatic: up to 16 blocks per SM, one block per warp (the caller pulls
-  // or pipelines them); beyond that, as few blocks per warp (at least 2) as
-  // keep about 24 latency-bound warps per SM, since the lanes of a warp
-  // diverge.
+  // Automatic: up to 48 blocks per SM, one block per chain (the caller
+  // pulls or pipelines them); beyond that, as few blocks per warp (at least
+  // 2) as keep about 24 latency-bound warps per SM, since the lanes of a
+  // warp diverge.
   if (bpw <= 0 || bpw > 32) {
     const uint32_t sms = (uint32_t)num_sms;
-    if (a.nblocks <= sms * 16u) return 1;
+    if (a.nblocks <= sms * 48u) return 1;
     bpw = (int)std::min<uint32_t>(32u, std::max<uint32_t>(2u, (a.nblocks + sms * 24u - 1) / (sms * 24u)));
   }
   return bpw;
@@ -1079,16 +1100,21 @@ void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st) {
   t1_mq_kernel<<<(a.nblocks + per_cta - 1) / per_cta, kMqWarps * 32, 0, st>>>(a, bpw);
 }
 
-void launch_t1_mq_pipe(const T1Args& a, int num_sms, int pipes_per_sm, uint32_t heavy, uint32_t* next,
+void launch_t1_mq_pipe(const T1Args& a, int num_sms, int pipes_per_sm, int chains, uint32_t heavy, uint32_t* next,
                        cudaStream_t st) {
   if (a.nblocks == 0) return;
   cudaMemsetAsync(next, 0, sizeof(uint32_t), st);
   heavy = heavy == 0 ? a.nblocks : std::min(heavy, a.nblocks);
+  const uint32_t per_pipe_cta = (uint32_t)kPipes * (chains == 2 ? 2u : 1u);  // blocks a CTA codes at once
   const uint32_t pipe_ctas = std::max<uint32_t>(
-      1u, std::min<uint32_t>((uint32_t)num_sms * (uint32_t)pipes_per_sm / kPipes, (heavy + kPipes - 1) / kPipes));
+      1u, std::min<uint32_t>((uint32_t)num_sms * (uint32_t)pipes_per_sm / kPipes,
+                             (heavy + per_pipe_cta - 1) / per_pipe_cta));
   const uint32_t per_cta = kPipes * 2 * 32;
   const uint32_t packed_ctas = (a.nblocks - heavy + per_cta - 1) / per_cta;
-  t1_mq_pipe_kernel<<<pipe_ctas + packed_ctas, kPipes * 64, 0, st>>>(a, next, pipe_ctas, heavy);
+  if (chains == 2)
+    t1_mq_pipe_kernel<2><<<pipe_ctas + packed_ctas, kPipes * 64, 0, st>>>(a, next, pipe_ctas, heavy);
+  else
+    t1_mq_pipe_kernel<1><<<pipe_ctas + packed_ctas, kPipes * 64, 0, st>>>(a, next, pipe_ctas, heavy);
 }
 
 void launch_t1_mq_pull(const T1Args& a, int num_sms, int warps_per_sm, uint32_t* next, cudaStream_t st) {

@@ -175,18 +175,22 @@ def test_server_and_batch_encoder_api(eng):
     assert enc.encoded_count() == 2
 
 
-@pytest.mark.parametrize("wps,pipes,heavy", [(-1, 0, 0), (1, -1, 0), (8, -1, 0), (64, -1, 0), (0, 1, 0),
-                                             (0, 4, 0), (0, 32, 0), (0, 4, 1), (0, 2, 37)])
+@pytest.mark.parametrize("wps,pipes,heavy,chains", [(-1, 0, 0, 0), (1, -1, 0, 0), (8, -1, 0, 0), (64, -1, 0, 0),
+                                                    (0, 1, 0, 0), (0, 4, 0, 0), (0, 32, 0, 0), (0, 4, 1, 0),
+                                                    (0, 2, 37, 0), (0, 1, 0, 2), (0, 8, 0, 2), (0, 32, 0, 2),
+                                                    (0, 4, 3, 2), (0, 2, 37, 2)])
 @pytest.mark.parametrize("q", [85, 100, 20])
-def test_mq_schedules_do_not_change_output(eng, orc, wps, pipes, heavy, q):
-    # static warps, single-warp pulling, producer/consumer pipelines, and
-    # pipelines for the heaviest blocks with the rest packed 32 to a warp
+def test_mq_schedules_do_not_change_output(eng, orc, wps, pipes, heavy, chains, q):
+    # static warps, single-warp pulling, producer/consumer pipelines with one
+    # or two chains per pair, and pipelines for the heaviest blocks with the
+    # rest packed 32 to a warp
     w, h = 600, 500
     px = synth_page(w, h, 1, 91, photo_w=200, photo_h=150)
-    opts = (_native.OPT_MQ_WARPS_PER_SM, _native.OPT_MQ_PIPES_PER_SM, _native.OPT_MQ_HEAVY)
+    opts = (_native.OPT_MQ_WARPS_PER_SM, _native.OPT_MQ_PIPES_PER_SM, _native.OPT_MQ_HEAVY,
+            _native.OPT_MQ_CHAINS_PER_PAIR)
     old = [eng.get_option(o) for o in opts]
     try:
-        for o, v in zip(opts, (wps, pipes, heavy)):
+        for o, v in zip(opts, (wps, pipes, heavy, chains)):
             eng.set_option(o, v)
         assert eng.encode(px, w, h, 1, q, 1) == orc.encode(px, w, h, 1, q, 1)
     finally:
