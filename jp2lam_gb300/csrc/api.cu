@@ -397,12 +397,12 @@ int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live) {
 // Code-blocks each MQ producer/consumer pair codes at once. Automatic: one
 // (all lanes on the chain) up to 8 blocks per SM, where the heaviest
 // block's chain sets the time; two (one per half-warp) above, where
-// instruction issue does (measured on 1700x2200 to 3400x4400 gray pages and
-// a 2550x3300 sRGB page).
+// instruction issue does (measured on gray pages of 1275x1650 to 3400x4400
+// and a 2550x3300 sRGB page).
 int mq_chains_per_pair(const jp2g_ctx* c, uint32_t nb) {
   const int64_t v = c->opt[JP2G_OPT_MQ_CHAINS_PER_PAIR];
   if (v == 1 || v == 2) return (int)v;
-  return nb > (uint32_t)c->num_sms * 8u ? 2 : 1;
+  return nb <= (uint32_t)c->num_sms * 8u ? 1 : 2;
 }
 
 // Runs f(0..n-1) on up to `threads` host threads.

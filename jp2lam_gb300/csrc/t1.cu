@@ -847,7 +847,7 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int half = lane / HL, hl = lane % HL;  // this lane's chain, its lane within it
-  const uint32_t hmask = H == 1 ? 0xffffffffu : (0xffffu << (16 * half));
+  const uint32_t hmask = H == 1 ? 0xffffffffu : (((1u << HL) - 1u) << (HL * half));
   // producers are warps 0..kPipes-1 and consumers the warps above, so the
   // (heavier) producer chains spread over the SM's schedulers
   const int pipe = warp % kPipes;
@@ -1105,7 +1105,8 @@ void launch_t1_mq_pipe(const T1Args& a, int num_sms, int pipes_per_sm, int chain
   if (a.nblocks == 0) return;
   cudaMemsetAsync(next, 0, sizeof(uint32_t), st);
   heavy = heavy == 0 ? a.nblocks : std::min(heavy, a.nblocks);
-  const uint32_t per_pipe_cta = (uint32_t)kPipes * (chains == 2 ? 2u : 1u);  // blocks a CTA codes at once
+  chains = chains == 2 ? 2 : 1;
+  const uint32_t per_pipe_cta = (uint32_t)kPipes * (uint32_t)chains;  // blocks a CTA codes at once
   const uint32_t pipe_ctas = std::max<uint32_t>(
       1u, std::min<uint32_t>((uint32_t)num_sms * (uint32_t)pipes_per_sm / kPipes,
                              (heavy + per_pipe_cta - 1) / per_pipe_cta));

@@ -237,3 +237,26 @@ def test_wave_size_is_capped_to_addressable_payload_slots(eng):
         eng.set_option(_native.OPT_WAVE_BLOCKS, old)
     assert all(isinstance(o, bytes) for o in outs)
     assert outs[:2] == ref
+
+
+@pytest.mark.parametrize("chains", [1, 2])
+def test_pipelines_with_many_blocks_per_chain_are_deterministic(eng, chains):
+    # a wave of ~12k code-blocks forced through the pipelines: every chain
+    # codes several blocks in turn; repeated encodes and one chain per pair
+    # must give the same bytes
+    pages = [{"px": synth_page(1275, 1650, 3 if i % 2 else 1, 7000 + i, photo_w=400, photo_h=300),
+              "w": 1275, "h": 1650, "ncomp": 3 if i % 2 else 1, "quality": (85, 50, 100)[i % 3], "fmt": 1}
+             for i in range(12)]
+    opts = (_native.OPT_MQ_BLOCKS_PER_WARP, _native.OPT_MQ_PIPES_PER_SM, _native.OPT_MQ_CHAINS_PER_PAIR)
+    old = [eng.get_option(o) for o in opts]
+    try:
+        for o, v in zip(opts, (1, 8, 1)):
+            eng.set_option(o, v)
+        ref = eng.encode_batch(pages)
+        eng.set_option(_native.OPT_MQ_CHAINS_PER_PAIR, chains)
+        assert eng.encode_batch(pages) == ref
+        assert eng.encode_batch(pages) == ref
+    finally:
+        for o, v in zip(opts, old):
+            eng.set_option(o, v)
+    assert ref[0] == _single(eng, pages[0])
