@@ -702,9 +702,10 @@ __device__ __forceinline__ void mq_code_block(const T1Args& a, uint32_t b, uint2
 // the second, so a producer warp runs it over 16-symbol chunks, handing each
 // symbol's (qe added to C | shift << 16) to a consumer warp that runs the C
 // chain, writes the bytes and records numbytes() at every pass end, one
-// chunk behind. All 32 lanes of each warp run the same chain (so the
-// barriers and the byte stores need no lane masks). Each pair of warps
-// pulls blocks, heaviest first, from an atomic counter.
+// chunk behind. All lanes of a chain (the whole warp, or one half-warp when
+// a pair codes two blocks at once) run the same chain on the same values, so
+// their byte stores coincide and only the chain's first lane writes the
+// handoff. Chains pull blocks, heaviest first, from an atomic counter.
 constexpr int kPipes = 4;  // pipelines (warp pairs) per CTA
 constexpr uint32_t kPipeEnd = 0xffffffffu;
 
