@@ -155,8 +155,10 @@ int jp2g_get_option(jp2g_ctx* ctx, int option, int64_t* value);
  * (1..100) encodes after one untimed encode. Every candidate must reproduce
  * the first encode's codestreams byte for byte; a difference, or a failed
  * encode, restores the previous options and returns JP2G_ENCODE_FAILED.
- * `best` (JP2G_NUM_OPTS entries) and `best_ms` may be NULL. No reference
- * counterpart: the reference has no tunable device schedule. */
+ * `best` (JP2G_NUM_OPTS entries) and `best_ms` may be NULL. The options it
+ * tries apply to the whole context, so call it while no submitted request is
+ * in flight. No reference counterpart: the reference has no tunable device
+ * schedule. */
 int jp2g_autotune(jp2g_ctx* ctx, const jp2g_request* reqs, uint32_t n, int repeats, int64_t* best,
                   double* best_ms);
 
