@@ -210,7 +210,10 @@ def _autotune(eng, dpages, args):
     if args.no_autotune:
         return defaults, None
     t0 = time.perf_counter()
-    best, ms = eng.autotune(dpages, repeats=1)
+    try:
+        best, ms = eng.autotune(dpages, repeats=1)
+    except Exception as e:  # the tuner restored the options; time under the defaults
+        return defaults, {"error": str(e), "options": None, "seconds": time.perf_counter() - t0}
     return defaults, {"options": {OPT_NAMES[o]: int(v) for o, v in best.items()},
                       "best_sample_ms": ms, "seconds": time.perf_counter() - t0,
                       "sample": "the workload's own pages, device-resident"}
