@@ -1309,7 +1309,8 @@ int jp2g_autotune(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, int repeats
                      "autotune: a scheduling setting changed the codestream (mq_blocks_per_warp=" +
                          std::to_string(o[JP2G_OPT_MQ_BLOCKS_PER_WARP]) + ", mq_warps_per_sm=" +
                          std::to_string(o[JP2G_OPT_MQ_WARPS_PER_SM]) + ", mq_pipes_per_sm=" +
-                         std::to_string(o[JP2G_OPT_MQ_PIPES_PER_SM]) + ", wave_blocks=" +
+                         std::to_string(o[JP2G_OPT_MQ_PIPES_PER_SM]) + ", mq_chains_per_pair=" +
+                         std::to_string(o[JP2G_OPT_MQ_CHAINS_PER_PAIR]) + ", wave_blocks=" +
                          std::to_string(o[JP2G_OPT_WAVE_BLOCKS]) + ")");
     return set_err(c, JP2G_ENCODE_FAILED, "autotune: the sample failed to encode: " + get_msg(c));
   };
