@@ -69,6 +69,7 @@ struct PageJob {
   std::vector<BlockKeep> keep;
   std::vector<uint32_t> offsets;  // nblocks + 1 body offsets
   std::vector<uint8_t> body;
+  const uint8_t* body_view = nullptr;  // the body in the host result buffer, when not copied
   std::vector<uint8_t> out;       // the codestream (J2K or JP2)
 };
 
@@ -523,8 +524,10 @@ size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
 // that fails validation or overflows a block slot is marked and the rest
 // carry on; a CUDA failure fails the wave (return code). `pre`: the wave's
 // host pixels already staged by stage_pixels (else they are staged here).
+// borrow_body: the pages' bodies stay in the host result buffer (the caller
+// assembles them before the next wave reuses it) instead of being copied.
 int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
-             const Prestaged* pre = nullptr) {
+             const Prestaged* pre = nullptr, bool borrow_body = false) {
   std::memset(c->counters, 0, sizeof c->counters);
   std::vector<PageJob*> live;
   int cbw = 0;
@@ -767,7 +770,13 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
     j->keep.assign(hk + b0, hk + b0 + n);
     j->offsets.resize((size_t)n + 1);
     for (uint32_t i = 0; i <= n; ++i) j->offsets[i] = hoff[b0 + i] - hoff[b0];
-    j->body.assign(hbody + hoff[b0], hbody + hoff[b0 + n]);
+    if (borrow_body) {
+      j->body.clear();
+      j->body_view = hbody + hoff[b0];
+    } else {
+      j->body.assign(hbody + hoff[b0], hbody + hoff[b0 + n]);
+      j->body_view = nullptr;
+    }
   }
   const BlockOut* hr = reinterpret_cast<const BlockOut*>(c->hres.p);
   c->counters[0] = nb;
@@ -787,12 +796,14 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
 void finish_page(PageJob* j) {
   if (j->status != kOk) return;
   Failure f{};
-  if (!assemble_codestream(j->plan, j->keep.data(), j->body.data(), j->offsets.data(), &j->out, &f)) {
+  const uint8_t* body = j->body_view ? j->body_view : j->body.data();
+  if (!assemble_codestream(j->plan, j->keep.data(), body, j->offsets.data(), &j->out, &f)) {
     j->status = f.code;
     j->err = f.msg;
   }
   j->body.clear();
   j->body.shrink_to_fit();
+  j->body_view = nullptr;
 }
 
 // Adds the device stages of the wave just run (events 0..6) to stage_ms.
@@ -829,7 +840,7 @@ void read_stage_times(jp2g_ctx* c) {
 // points).
 int encode_one(jp2g_ctx* c, PageJob* j, WaveDebug* dbg) {
   PageJob* jobs[1] = {j};
-  if (int rc = run_wave(c, jobs, 1, dbg)) return rc;
+  if (int rc = run_wave(c, jobs, 1, dbg, nullptr, true)) return rc;
   if (j->status != kOk) return set_err(c, j->status, j->err);
   if (dbg && dbg->stop_after_dwt) return kOk;
   finish_page(j);

@@ -25,8 +25,16 @@ class BitWriter {
     --free_;
     cur_ |= (b & 1u) << free_;
   }
+  // The n low bits of v, most significant first (as n calls of bit()), a
+  // byte's worth at a time.
   void bits(uint32_t v, int n) {
-    while (n-- > 0) bit((v >> n) & 1u);
+    while (n > 0) {
+      if (free_ == 0) next();
+      const int take = n < free_ ? n : free_;
+      n -= take;
+      free_ -= take;
+      cur_ |= ((v >> n) & ((1u << take) - 1u)) << free_;
+    }
   }
   void finish() {
     next();
@@ -163,8 +171,16 @@ static void packet_header(const PagePlan& p, size_t band_begin, size_t band_end,
 
 bool assemble_codestream(const PagePlan& p, const BlockKeep* keep, const uint8_t* body,
                          const uint32_t* offsets, std::vector<uint8_t>* out, Failure* err) {
-  std::vector<uint8_t> pay;
-  pay.reserve(offsets[p.nblocks] + 64 * (size_t)(p.levels + 1) * p.ncomp + 1024);
+  // Packet headers first (small), so every length is known before the
+  // output is laid out; then each byte of the output is written once.
+  std::vector<uint8_t> hdr;
+  hdr.reserve(64 * (size_t)(p.levels + 1) * p.ncomp + 1024);
+  struct Packet {
+    size_t hdr_end;       // end of the packet's header in hdr
+    uint32_t body0, body1;  // its body bytes in `body`
+  };
+  std::vector<Packet> packets;
+  uint64_t pay = 0;
   // bands are stored res -> comp -> orient, i.e. already in packet order
   size_t bi = 0;
   while (bi < p.bands.size()) {
@@ -172,100 +188,120 @@ bool assemble_codestream(const PagePlan& p, const BlockKeep* keep, const uint8_t
     while (be < p.bands.size() && p.bands[be].res == p.bands[bi].res &&
            p.bands[be].comp == p.bands[bi].comp)
       ++be;
-    packet_header(p, bi, be, keep, &pay);
-    uint32_t b0 = p.bands[bi].first_block;
+    packet_header(p, bi, be, keep, &hdr);
+    const uint32_t b0 = p.bands[bi].first_block;
     const BandGeom& last = p.bands[be - 1];
-    uint32_t b1 = last.first_block + (uint32_t)(last.ncbx * last.ncby);
-    pay.insert(pay.end(), body + offsets[b0], body + offsets[b1]);
+    const uint32_t b1 = last.first_block + (uint32_t)(last.ncbx * last.ncby);
+    packets.push_back({hdr.size(), offsets[b0], offsets[b1]});
+    pay += offsets[b1] - offsets[b0];
     bi = be;
   }
-  std::vector<uint8_t>& o = *out;
-  o.clear();
-  o.reserve(pay.size() + 256);
-  be16(o, 0xff4f);  // SOC
-  be16(o, 0xff51);  // SIZ
-  be16(o, 38 + 3 * p.ncomp);
-  be16(o, 0);
-  be32(o, p.width);
-  be32(o, p.height);
-  be32(o, 0);
-  be32(o, 0);
-  be32(o, p.width);
-  be32(o, p.height);
-  be32(o, 0);
-  be32(o, 0);
-  be16(o, p.ncomp);
+  pay += hdr.size();
+
+  // main header, SOT and SOD
+  std::vector<uint8_t> mh;
+  mh.reserve(256);
+  be16(mh, 0xff4f);  // SOC
+  be16(mh, 0xff51);  // SIZ
+  be16(mh, 38 + 3 * p.ncomp);
+  be16(mh, 0);
+  be32(mh, p.width);
+  be32(mh, p.height);
+  be32(mh, 0);
+  be32(mh, 0);
+  be32(mh, p.width);
+  be32(mh, p.height);
+  be32(mh, 0);
+  be32(mh, 0);
+  be16(mh, p.ncomp);
   for (int c = 0; c < p.ncomp; ++c) {
-    o.push_back((uint8_t)((p.precision - 1) & 0x7f));
-    o.push_back(1);
-    o.push_back(1);
+    mh.push_back((uint8_t)((p.precision - 1) & 0x7f));
+    mh.push_back(1);
+    mh.push_back(1);
   }
-  be16(o, 0xff52);  // COD
-  be16(o, 12);
-  o.push_back(0);  // Scod
-  o.push_back(0);  // LRCP
-  be16(o, 1);      // one layer
-  o.push_back(p.use_mct ? 1 : 0);
-  o.push_back((uint8_t)p.levels);
-  o.push_back((uint8_t)(__builtin_ctz((unsigned)p.cbw) - 2));
-  o.push_back((uint8_t)(__builtin_ctz((unsigned)p.cbh) - 2));
-  o.push_back(0);
-  o.push_back(p.lossless ? 1 : 0);
-  be16(o, 0xff5c);  // QCD
+  be16(mh, 0xff52);  // COD
+  be16(mh, 12);
+  mh.push_back(0);  // Scod
+  mh.push_back(0);  // LRCP
+  be16(mh, 1);      // one layer
+  mh.push_back(p.use_mct ? 1 : 0);
+  mh.push_back((uint8_t)p.levels);
+  mh.push_back((uint8_t)(__builtin_ctz((unsigned)p.cbw) - 2));
+  mh.push_back((uint8_t)(__builtin_ctz((unsigned)p.cbh) - 2));
+  mh.push_back(0);
+  mh.push_back(p.lossless ? 1 : 0);
+  be16(mh, 0xff5c);  // QCD
   if (p.lossless) {
-    be16(o, 3 + (uint32_t)p.quants.size());
-    o.push_back((uint8_t)(p.guard_bits << 5));
-    for (const auto& q : p.quants) o.push_back((uint8_t)(q.exponent << 3));
+    be16(mh, 3 + (uint32_t)p.quants.size());
+    mh.push_back((uint8_t)(p.guard_bits << 5));
+    for (const auto& q : p.quants) mh.push_back((uint8_t)(q.exponent << 3));
   } else {
-    be16(o, 3 + 2 * (uint32_t)p.quants.size());
-    o.push_back((uint8_t)((p.guard_bits << 5) | 2));
-    for (const auto& q : p.quants) be16(o, (((uint32_t)q.exponent & 0xffu) << 11 | ((uint32_t)q.mantissa & 0x7ffu)) & 0xffffu);
+    be16(mh, 3 + 2 * (uint32_t)p.quants.size());
+    mh.push_back((uint8_t)((p.guard_bits << 5) | 2));
+    for (const auto& q : p.quants) be16(mh, (((uint32_t)q.exponent & 0xffu) << 11 | ((uint32_t)q.mantissa & 0x7ffu)) & 0xffffu);
   }
-  uint64_t psot = 12 + 2 + (uint64_t)pay.size();
+  const uint64_t psot = 12 + 2 + pay;
   if (psot > 0xffffffffull) {
     *err = {kEncodeFailed, "tile-part length exceeds Psot range"};
     return false;
   }
-  be16(o, 0xff90);  // SOT
-  be16(o, 10);
-  be16(o, 0);
-  be32(o, (uint32_t)psot);
-  o.push_back(0);
-  o.push_back(1);
-  be16(o, 0xff93);  // SOD
-  o.insert(o.end(), pay.begin(), pay.end());
-  be16(o, 0xffd9);  // EOC
+  be16(mh, 0xff90);  // SOT
+  be16(mh, 10);
+  be16(mh, 0);
+  be32(mh, (uint32_t)psot);
+  mh.push_back(0);
+  mh.push_back(1);
+  be16(mh, 0xff93);  // SOD
+  const uint64_t cs_len = mh.size() + pay + 2;  // + EOC
+
+  // JP2 boxes ahead of the codestream (src/jp2.rs:13-71)
+  std::vector<uint8_t> boxes;
   if (p.format == 1) {
-    std::vector<uint8_t> j;
-    uint64_t jl = (uint64_t)o.size() + 8;
+    const uint64_t jl = cs_len + 8;
     if (jl > 0xffffffffull) {
       *err = {kEncodeFailed, "JP2 box length exceeds 32-bit limit"};
       return false;
     }
-    j.reserve(o.size() + 85);
+    boxes.reserve(96);
     auto box = [&](uint32_t len, const char* t) {
-      be32(j, len);
-      j.insert(j.end(), t, t + 4);
+      be32(boxes, len);
+      boxes.insert(boxes.end(), t, t + 4);
     };
     box(12, "jP  ");
-    j.insert(j.end(), {0x0d, 0x0a, 0x87, 0x0a});
+    boxes.insert(boxes.end(), {0x0d, 0x0a, 0x87, 0x0a});
     box(20, "ftyp");
-    j.insert(j.end(), {'j', 'p', '2', ' '});
-    be32(j, 0);
-    j.insert(j.end(), {'j', 'p', '2', ' '});
+    boxes.insert(boxes.end(), {'j', 'p', '2', ' '});
+    be32(boxes, 0);
+    boxes.insert(boxes.end(), {'j', 'p', '2', ' '});
     box(8 + 22 + 15, "jp2h");
     box(22, "ihdr");
-    be32(j, p.height);
-    be32(j, p.width);
-    be16(j, p.ncomp);
-    j.insert(j.end(), {7, 7, 0, 0});  // BPC, compression type 7, UnkC, IPR
+    be32(boxes, p.height);
+    be32(boxes, p.width);
+    be16(boxes, p.ncomp);
+    boxes.insert(boxes.end(), {7, 7, 0, 0});  // BPC, compression type 7, UnkC, IPR
     box(15, "colr");
-    j.insert(j.end(), {1, 0, 0});
-    be32(j, p.srgb ? 16 : 17);
+    boxes.insert(boxes.end(), {1, 0, 0});
+    be32(boxes, p.srgb ? 16 : 17);
     box((uint32_t)jl, "jp2c");
-    j.insert(j.end(), o.begin(), o.end());
-    o.swap(j);
   }
+
+  std::vector<uint8_t>& o = *out;
+  o.resize(boxes.size() + cs_len);
+  uint8_t* w = o.data();
+  auto put = [&](const uint8_t* src, size_t n) {
+    if (n) std::memcpy(w, src, n);
+    w += n;
+  };
+  put(boxes.data(), boxes.size());
+  put(mh.data(), mh.size());
+  size_t h0 = 0;
+  for (const Packet& k : packets) {
+    put(hdr.data() + h0, k.hdr_end - h0);
+    put(body + k.body0, k.body1 - k.body0);
+    h0 = k.hdr_end;
+  }
+  const uint8_t eoc[2] = {0xff, 0xd9};
+  put(eoc, 2);
   return true;
 }
 
