@@ -149,12 +149,13 @@ int jp2g_get_option(jp2g_ctx* ctx, int option, int64_t* value);
 /* Autotuner: encodes the caller's sample pages (through jp2g_encode_batch)
  * under each candidate setting of the MQ schedule (automatic; 4, 8 or 16
  * producer/consumer pairs per SM with one or two chains each; 8, 12 or 16
- * pulling warps per SM; 2 to 32 blocks packed per warp), then of the wave size (20,000 to 240,000
- * code-blocks) under the fastest schedule, and leaves the fastest setting on
- * the context. A candidate's time is the least wall time of `repeats`
- * (1..100) encodes after one untimed encode. Every candidate must reproduce
- * the first encode's codestreams byte for byte; a difference, or a failed
- * encode, restores the previous options and returns JP2G_ENCODE_FAILED.
+ * pulling warps per SM; 2 to 32 blocks packed per warp), then of the wave
+ * size (20,000 to 240,000 code-blocks) under the fastest schedule, and
+ * leaves the fastest setting on the context. A candidate's time is the least
+ * wall time of `repeats` (1..100) encodes after one untimed encode. Every
+ * candidate must reproduce the first encode's codestreams byte for byte; a
+ * difference, or a failed encode, restores the previous options and returns
+ * JP2G_ENCODE_FAILED.
  * `best` (JP2G_NUM_OPTS entries) and `best_ms` may be NULL. The options it
  * tries apply to the whole context, so call it while no submitted request is
  * in flight. No reference counterpart: the reference has no tunable device
@@ -197,6 +198,14 @@ int jp2g_debug_coefficients(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32
 int jp2g_debug_blocks(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,
                       uint32_t ncomp, uint8_t quality, int32_t* rows, uint32_t cap,
                       uint32_t* nblocks);
+/* Host Tier-2 alone (no context, no device): packet headers, markers and
+ * JP2 boxes of a w x h page whose nblocks code-blocks, in codestream order
+ * (resolution, component, band, raster), retain npasses[i] passes in one
+ * segment of seg_len[i] bytes, consecutive in `body`, above zbp[i] zero
+ * bit-planes. *out is malloc'd (free with jp2g_free). */
+int jp2g_debug_assemble(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int format,
+                        const uint16_t* npasses, const uint8_t* zbp, const uint32_t* seg_len,
+                        const uint8_t* body, uint32_t nblocks, uint8_t** out, size_t* out_len);
 
 /* Allocation-free first stage of the encoder: level shift + RCT/ICT, every
  * DWT level and the deadzone quantiser, for callers that cannot allocate

@@ -51,7 +51,7 @@ EXPORTS = [
     "jp2g_last_error", "jp2g_stream", "jp2g_set_timing", "jp2g_stage_times", "jp2g_counters",
     "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
     "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
-    "jp2g_autotune",
+    "jp2g_autotune", "jp2g_debug_assemble",
 ]
 
 PENDING = 6
@@ -121,6 +121,10 @@ def load_library(path: str = LIB_PATH):
         lib.jp2g_get_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
         lib.jp2g_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_uint32, ctypes.c_int,
                                       ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)]
+        lib.jp2g_debug_assemble.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8,
+                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(_u8p),
+                                            ctypes.POINTER(ctypes.c_size_t)]
         _lib = lib
         return lib
 
@@ -324,6 +328,31 @@ def tables():
     mq = np.zeros(94, np.uint32)
     lib.jp2g_tables(*(a.ctypes.data_as(ctypes.c_void_p) for a in (zc, sc, spb, mq)))
     return zc, sc, spb, mq
+
+
+def debug_assemble(w: int, h: int, ncomp: int, quality: int, fmt: int, npasses, zbp, seg_len,
+                   body) -> bytes:
+    """Host Tier-2 alone (host-only, no GPU needed): the codestream of a page
+    whose code-blocks, in codestream order, retain npasses[i] passes in one
+    segment of seg_len[i] bytes (consecutive in body) above zbp[i] zero
+    bit-planes."""
+    lib = load_library()
+    npasses = np.ascontiguousarray(npasses, dtype=np.uint16)
+    zbp = np.ascontiguousarray(zbp, dtype=np.uint8)
+    seg_len = np.ascontiguousarray(seg_len, dtype=np.uint32)
+    body = np.ascontiguousarray(np.frombuffer(bytes(body), np.uint8) if not isinstance(body, np.ndarray) else body,
+                                dtype=np.uint8)
+    out = _u8p()
+    n = ctypes.c_size_t()
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    rc = lib.jp2g_debug_assemble(w, h, ncomp, quality, fmt, ptr(npasses), ptr(zbp), ptr(seg_len),
+                                 ptr(body) if body.size else None, len(npasses), ctypes.byref(out),
+                                 ctypes.byref(n))
+    if rc != 0:
+        _raise(rc, "host Tier-2 assembly failed")
+    data = ctypes.string_at(out, n.value)
+    lib.jp2g_free(out)
+    return data
 
 
 _default = None

@@ -1461,6 +1461,35 @@ int jp2g_debug_blocks(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, ui
   return JP2G_OK;
 }
 
+int jp2g_debug_assemble(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int format,
+                        const uint16_t* npasses, const uint8_t* zbp, const uint32_t* seg_len,
+                        const uint8_t* body, uint32_t nblocks, uint8_t** out, size_t* out_len) {
+  if (!out || !out_len || (nblocks > 0 && (!npasses || !zbp || !seg_len))) return JP2G_INVALID_INPUT;
+  PagePlan p;
+  Failure f{};
+  if (!build_plan(w, h, (int)ncomp, quality, format, &p, &f)) return f.code;
+  if (nblocks != p.nblocks) return JP2G_INVALID_INPUT;
+  std::vector<BlockKeep> keep(nblocks);
+  std::vector<uint32_t> offsets((size_t)nblocks + 1, 0);
+  for (uint32_t i = 0; i < nblocks; ++i) {
+    BlockKeep k{};
+    k.npasses = npasses[i];
+    k.zbp = zbp[i];
+    k.seg_len = npasses[i] ? seg_len[i] : 0;
+    k.body_len = k.seg_len;
+    keep[i] = k;
+    offsets[i + 1] = offsets[i] + k.body_len;
+  }
+  if (offsets[nblocks] > 0 && !body) return JP2G_INVALID_INPUT;
+  std::vector<uint8_t> cs;
+  if (!assemble_codestream(p, keep.data(), body, offsets.data(), &cs, &f)) return f.code;
+  *out = static_cast<uint8_t*>(std::malloc(std::max<size_t>(cs.size(), 1)));
+  if (!*out) return JP2G_ENCODE_FAILED;
+  std::memcpy(*out, cs.data(), cs.size());
+  *out_len = cs.size();
+  return JP2G_OK;
+}
+
 // Host-only: the Tier-1 tables the device uses, for checking against the
 // reference's literal tables without a GPU.
 void jp2g_tables(uint8_t* zc, uint8_t* sc, uint8_t* spb, uint32_t* mq) {

@@ -155,6 +155,12 @@ std::vector<uint8_t> build_payload(const std::vector<Layout>& layouts);
 std::vector<uint8_t> build_codestream(const Plan& p,
                                       const std::vector<uint8_t>& payload);
 std::vector<uint8_t> wrap_jp2(const Plan& p, const std::vector<uint8_t>& cs);
+// Layouts of a page whose code-blocks, taken in codestream order (resolution,
+// component, band, raster), retain npasses[i] passes in one terminated
+// segment of seg_len[i] bytes from `body`, above zbp[i] zero bit-planes:
+// the geometry of tier1_layouts without running Tier-1.
+std::vector<Layout> layouts_from_blocks(const Plan& p, const uint16_t* npasses, const uint8_t* zbp,
+                                        const uint32_t* seg_len, const uint8_t* body, uint32_t nblocks);
 
 // --- decoder (parity checker for round trips) --------------------------------
 struct Decoded {

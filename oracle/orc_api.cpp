@@ -58,6 +58,24 @@ int orc_encode(const uint8_t* px, uint32_t w, uint32_t h, int ncomp, int quality
   }
 }
 
+// Tier-2, markers and JP2 boxes of a page from per-block retained data in
+// codestream order (see layouts_from_blocks); the bodies are consecutive in
+// `body`.
+int orc_assemble(uint32_t w, uint32_t h, int ncomp, int quality, int format, const uint16_t* npasses,
+                 const uint8_t* zbp, const uint32_t* seg_len, const uint8_t* body, uint32_t nblocks,
+                 uint8_t** out, size_t* out_len) {
+  if (int rc = check_input(w, h, ncomp)) return rc;
+  try {
+    orc::Plan p = orc::build_plan(w, h, ncomp, quality, format);
+    auto layouts = orc::layouts_from_blocks(p, npasses, zbp, seg_len, body, nblocks);
+    auto cs = orc::build_codestream(p, orc::build_payload(layouts));
+    *out = dup(format == 1 ? orc::wrap_jp2(p, cs) : cs, out_len);
+    return 0;
+  } catch (const orc::Error& e) {
+    return fail(e);
+  }
+}
+
 // Quantised coefficient plane of one component (Mallat layout, W*H int32).
 int orc_coefficients(const uint8_t* px, uint32_t w, uint32_t h, int ncomp,
                      int quality, int comp, int32_t* out) {

@@ -295,6 +295,52 @@ std::vector<Layout> tier1_layouts(const Plan& p, const Planes& px,
   return layouts;
 }
 
+std::vector<Layout> layouts_from_blocks(const Plan& p, const uint16_t* npasses, const uint8_t* zbp,
+                                        const uint32_t* seg_len, const uint8_t* body, uint32_t nblocks) {
+  std::vector<Layout> layouts(p.ncomp);
+  auto rects = band_rects(p.width, p.height, p.levels);
+  for (int c = 0; c < p.ncomp; ++c)
+    for (const auto& r : rects) {
+      EncBand b{r.res, r.band, {}};
+      // split_codeblocks (layout.rs:120-159)
+      for (int by = r.y0; by < r.y1; by = std::min(by + p.cbh, r.y1))
+        for (int bx = r.x0; bx < r.x1; bx = std::min(bx + p.cbw, r.x1)) {
+          EncBlock e{};
+          e.res = r.res;
+          e.band = r.band;
+          e.x0 = bx; e.y0 = by; e.x1 = std::min(bx + p.cbw, r.x1); e.y1 = std::min(by + p.cbh, r.y1);
+          b.blocks.push_back(std::move(e));
+        }
+      layouts[c].push_back(std::move(b));
+    }
+  // codestream order: resolution, then component, then the component's
+  // bands of that resolution, then raster order within a band
+  int maxr = 0;
+  for (const auto& r : rects) maxr = std::max(maxr, r.res);
+  uint32_t k = 0;
+  size_t at = 0;
+  for (int res = 0; res <= maxr; ++res)
+    for (int c = 0; c < p.ncomp; ++c)
+      for (auto& band : layouts[c]) {
+        if (band.res != res) continue;
+        for (auto& e : band.blocks) {
+          if (k >= nblocks) throw Error(kInvalidInput, "fewer block records than code-blocks");
+          e.zbp = zbp[k];
+          for (uint32_t i = 0; i < npasses[k]; ++i) {
+            Pass ps{};
+            ps.terminated = i + 1 == npasses[k];
+            ps.length = ps.terminated ? seg_len[k] : 0;
+            e.passes.push_back(ps);
+          }
+          if (npasses[k] > 0) e.payload.assign(body + at, body + at + seg_len[k]);
+          at += npasses[k] > 0 ? seg_len[k] : 0;
+          ++k;
+        }
+      }
+  if (k != nblocks) throw Error(kInvalidInput, "more block records than code-blocks");
+  return layouts;
+}
+
 // ------------------------------------------------------------------ T2 -----
 struct Bio {  // src/encode/backend/native/t2.rs:25-67
   std::vector<uint8_t> buf;

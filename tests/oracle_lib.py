@@ -41,6 +41,24 @@ class Oracle:
         self.lib.orc_free(out)
         return data
 
+    def assemble(self, w, h, ncomp, quality, fmt, npasses, zbp, seg_len, body):
+        """Tier-2, markers and JP2 boxes from per-block retained data in
+        codestream order (the oracle's own layout geometry)."""
+        npasses = np.ascontiguousarray(npasses, dtype=np.uint16)
+        zbp = np.ascontiguousarray(zbp, dtype=np.uint8)
+        seg_len = np.ascontiguousarray(seg_len, dtype=np.uint32)
+        body = np.ascontiguousarray(body, dtype=np.uint8)
+        out = _u8p()
+        n = ctypes.c_size_t()
+        ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        rc = self.lib.orc_assemble(ctypes.c_uint32(w), ctypes.c_uint32(h), ncomp, quality, fmt, ptr(npasses),
+                                   ptr(zbp), ptr(seg_len), ptr(body) if body.size else None,
+                                   ctypes.c_uint32(len(npasses)), ctypes.byref(out), ctypes.byref(n))
+        self._err(rc, "orc_assemble")
+        data = ctypes.string_at(out, n.value)
+        self.lib.orc_free(out)
+        return data
+
     def coefficients(self, px, w, h, ncomp, quality, comp):
         px = np.ascontiguousarray(px, dtype=np.uint8)
         out = np.zeros(w * h, np.int32)
