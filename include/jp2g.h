@@ -206,6 +206,12 @@ int jp2g_debug_blocks(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,
 int jp2g_debug_assemble(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int format,
                         const uint16_t* npasses, const uint8_t* zbp, const uint32_t* seg_len,
                         const uint8_t* body, uint32_t nblocks, uint8_t** out, size_t* out_len);
+/* Encoding plan alone (no context, no device), as EncodingPlan::build makes
+ * it (src/plan/mod.rs:116-177): decomposition levels, code-block width,
+ * quantiser entries (up to 32, as (resolution, band, exponent, mantissa)),
+ * code-blocks of the page, and the PCRD lambda at `quality` and at 1. */
+int jp2g_debug_plan(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int* levels, int* cbw,
+                    int* nquant, int* quants, uint32_t* nblocks, double* lambdas);
 
 /* Allocation-free first stage of the encoder: level shift + RCT/ICT, every
  * DWT level and the deadzone quantiser, for callers that cannot allocate

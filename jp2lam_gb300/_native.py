@@ -51,7 +51,7 @@ EXPORTS = [
     "jp2g_last_error", "jp2g_stream", "jp2g_set_timing", "jp2g_stage_times", "jp2g_counters",
     "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
     "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
-    "jp2g_autotune", "jp2g_debug_assemble",
+    "jp2g_autotune", "jp2g_debug_assemble", "jp2g_debug_plan",
 ]
 
 PENDING = 6
@@ -121,6 +121,10 @@ def load_library(path: str = LIB_PATH):
         lib.jp2g_get_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
         lib.jp2g_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_uint32, ctypes.c_int,
                                       ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)]
+        lib.jp2g_debug_plan.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8,
+                                        ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                        ctypes.POINTER(ctypes.c_int), ctypes.c_void_p,
+                                        ctypes.POINTER(ctypes.c_uint32), ctypes.c_void_p]
         lib.jp2g_debug_assemble.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8,
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(_u8p),
@@ -353,6 +357,22 @@ def debug_assemble(w: int, h: int, ncomp: int, quality: int, fmt: int, npasses, 
     data = ctypes.string_at(out, n.value)
     lib.jp2g_free(out)
     return data
+
+
+def debug_plan(w: int, h: int, ncomp: int, quality: int) -> dict:
+    """The encoding plan (host-only, no GPU needed): levels, code-block
+    width, quantiser entries (res, band, exponent, mantissa), code-blocks and
+    the PCRD lambdas at the quality and at 1."""
+    lib = load_library()
+    lv, cbw, nq, nb = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_uint32()
+    q = np.zeros(4 * 32, np.int32)
+    lam = np.zeros(2, np.float64)
+    rc = lib.jp2g_debug_plan(w, h, ncomp, quality, ctypes.byref(lv), ctypes.byref(cbw), ctypes.byref(nq),
+                             q.ctypes.data_as(ctypes.c_void_p), ctypes.byref(nb), lam.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        _raise(rc, "plan failed")
+    return {"levels": lv.value, "cbw": cbw.value, "quants": [tuple(q[4 * i:4 * i + 4]) for i in range(nq.value)],
+            "nblocks": nb.value, "lambdas": (float(lam[0]), float(lam[1]))}
 
 
 _default = None

@@ -1490,6 +1490,27 @@ int jp2g_debug_assemble(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality,
   return JP2G_OK;
 }
 
+int jp2g_debug_plan(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int* levels, int* cbw,
+                    int* nquant, int* quants, uint32_t* nblocks, double* lambdas) {
+  if (!levels || !cbw || !nquant || !quants || !nblocks || !lambdas) return JP2G_INVALID_INPUT;
+  PagePlan p;
+  Failure f{};
+  if (!build_plan(w, h, (int)ncomp, quality, 0, &p, &f)) return f.code;
+  *levels = p.levels;
+  *cbw = p.cbw;
+  *nquant = (int)p.quants.size();
+  for (size_t i = 0; i < p.quants.size() && i < 32; ++i) {
+    quants[4 * i + 0] = p.quants[i].res;
+    quants[4 * i + 1] = p.quants[i].orient;
+    quants[4 * i + 2] = p.quants[i].exponent;
+    quants[4 * i + 3] = p.quants[i].mantissa;
+  }
+  *nblocks = p.nblocks;
+  lambdas[0] = p.lambda_raw;
+  lambdas[1] = p.lambda_floor;
+  return JP2G_OK;
+}
+
 // Host-only: the Tier-1 tables the device uses, for checking against the
 // reference's literal tables without a GPU.
 void jp2g_tables(uint8_t* zc, uint8_t* sc, uint8_t* spb, uint32_t* mq) {

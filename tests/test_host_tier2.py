@@ -2,8 +2,8 @@
 trees, Table B-4 pass counts, Lblock comma codes and 0xFF stuffing; SIZ, COD,
 QCD, SOT, SOD, EOC; JP2 boxes) against the oracle's restatement of
 src/encode/backend/native/t2.rs:337-473, src/j2k/write.rs:9-77 and
-src/jp2.rs:13-71, on random per-block retained data. No GPU: both sides take
-the same block records and bodies."""
+src/jp2.rs:13-71, on random per-block retained data, and of its encoding
+plan. No GPU: both sides take the same inputs."""
 import numpy as np
 import pytest
 
@@ -54,3 +54,20 @@ def test_host_tier2_rejects_a_wrong_block_count(orc):
     rec = _records(n + 1, 5)
     with pytest.raises(_native.InvalidInput):
         _native.debug_assemble(100, 70, 1, 85, 0, *rec)
+
+
+@pytest.mark.parametrize("w,h,ncomp", [(1, 1, 1), (7, 33, 3), (64, 64, 1), (300, 257, 3), (2550, 3300, 1),
+                                        (2550, 3300, 3), (5100, 6600, 3), (256, 256, 1), (33, 1000, 1)])
+@pytest.mark.parametrize("quality", [1, 20, 29, 30, 50, 60, 75, 85, 90, 99, 100])
+def test_host_plan_matches_oracle(orc, w, h, ncomp, quality):
+    # levels, code-block size, quantiser entries (norms.rs:68-90,
+    # derive.rs:60-165), code-block count and the PCRD lambdas
+    # (pcrd.rs:1425-1456) that the device kernels are driven by
+    got = _native.debug_plan(w, h, ncomp, quality)
+    want = orc.plan(w, h, ncomp, quality)
+    assert got["levels"] == want["levels"]
+    assert got["cbw"] == want["cbw"]
+    assert [tuple(int(v) for v in q) for q in got["quants"]] == [tuple(int(v) for v in q) for q in want["quants"]]
+    assert got["nblocks"] == _block_count(orc, w, h, ncomp, quality)
+    f = orc.lib.orc_quality_to_lambda
+    assert got["lambdas"] == (f(quality, w * h), f(1, w * h))
