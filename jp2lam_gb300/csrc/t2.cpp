@@ -55,15 +55,18 @@ class BitWriter {
 };
 
 // Tag tree (ISO 15444-1 B.10.2) with explicit levels; node (i, j) of a level
-// has parent (i/2, j/2) in the next.
+// has parent (i/2, j/2) in the next. reset() keeps the storage, so one tree
+// per thread serves every band.
 class TagTree {
  public:
-  TagTree(int w, int h) {
+  void reset(int w, int h) {
     int lw = std::max(w, 1), lh = std::max(h, 1);
+    levels_ = 0;
+    total_ = 0;
     for (;;) {
-      lw_.push_back(lw);
-      lh_.push_back(lh);
-      off_.push_back(total_);
+      lw_[levels_] = lw;
+      off_[levels_] = total_;
+      ++levels_;
       total_ += lw * lh;
       if (lw * lh <= 1) break;
       lw = (lw + 1) / 2;
@@ -75,7 +78,7 @@ class TagTree {
   }
   void set(int leaf, int v) {
     int i = leaf % lw_[0], j = leaf / lw_[0];
-    for (size_t l = 0; l < lw_.size(); ++l, i >>= 1, j >>= 1) {
+    for (int l = 0; l < levels_; ++l, i >>= 1, j >>= 1) {
       int& cur = value_[off_[l] + j * lw_[l] + i];
       if (cur <= v) break;
       cur = v;
@@ -83,12 +86,11 @@ class TagTree {
   }
   void encode(BitWriter& bw, int leaf, int threshold) {
     int path[32];
-    int depth = 0;
     int i = leaf % lw_[0], j = leaf / lw_[0];
-    for (size_t l = 0; l < lw_.size(); ++l, i >>= 1, j >>= 1) path[depth++] = off_[l] + j * lw_[l] + i;
+    for (int l = 0; l < levels_; ++l, i >>= 1, j >>= 1) path[l] = off_[l] + j * lw_[l] + i;
     int low = 0;
-    for (int k = depth - 1; k >= 0; --k) {  // root first
-      int n = path[k];
+    for (int k = levels_ - 1; k >= 0; --k) {  // root first
+      const int n = path[k];
       if (low > low_[n]) low_[n] = low;
       else low = low_[n];
       while (low < threshold) {
@@ -107,9 +109,10 @@ class TagTree {
   }
 
  private:
-  std::vector<int> lw_, lh_, off_, value_, low_;
+  int lw_[32], off_[32];
+  int levels_ = 0, total_ = 0;
+  std::vector<int> value_, low_;
   std::vector<uint8_t> known_;
-  int total_ = 0;
 };
 
 int flog2(uint32_t v) { return v == 0 ? 0 : 31 - __builtin_clz(v); }
@@ -143,7 +146,9 @@ static void packet_header(const PagePlan& p, size_t band_begin, size_t band_end,
     const BandGeom& g = p.bands[bi];
     const int n = g.ncbx * g.ncby;
     if (n == 0) continue;
-    TagTree incl(g.ncbx, g.ncby), zbp(g.ncbx, g.ncby);
+    thread_local TagTree incl, zbp;
+    incl.reset(g.ncbx, g.ncby);
+    zbp.reset(g.ncbx, g.ncby);
     for (int i = 0; i < n; ++i) {
       const BlockKeep& k = keep[g.first_block + i];
       zbp.set(i, k.zbp);
