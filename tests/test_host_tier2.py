@@ -58,7 +58,7 @@ def test_host_tier2_rejects_a_wrong_block_count(orc):
 
 @pytest.mark.parametrize("w,h,ncomp", [(1, 1, 1), (7, 33, 3), (64, 64, 1), (300, 257, 3), (2550, 3300, 1),
                                         (2550, 3300, 3), (5100, 6600, 3), (256, 256, 1), (33, 1000, 1)])
-@pytest.mark.parametrize("quality", [1, 20, 29, 30, 50, 60, 75, 85, 90, 99, 100])
+@pytest.mark.parametrize("quality", [0, 1, 20, 29, 30, 50, 60, 75, 85, 90, 99, 100, 101, 255])
 def test_host_plan_matches_oracle(orc, w, h, ncomp, quality):
     # levels, code-block size, quantiser entries (norms.rs:68-90,
     # derive.rs:60-165), code-block count and the PCRD lambdas
