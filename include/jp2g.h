@@ -38,7 +38,13 @@ enum {
 enum { JP2G_FORMAT_J2K = 0, JP2G_FORMAT_JP2 = 1 };
 
 /* One engine per process and GPU. Owns a CUDA stream and device buffer pools
- * that grow on demand up to `hbm_budget_bytes` (0 = no limit).
+ * that grow on demand up to `hbm_budget_bytes` (0 = no limit). Under a
+ * budget, a device wave whose pools would not fit is retried from empty
+ * pools and then split in halves (recursively), and later waves are capped
+ * at the size that fitted; only a page that does not fit on its own fails
+ * (JP2G_ENCODE_FAILED, "device memory budget exhausted ..."). No
+ * jp2g_poll may be waiting when jp2g_destroy is called; queued requests are
+ * finished first.
  * Replaces the construction of NativeBackend (src/encode/backend/mod.rs:6-9;
  * src/encode/mod.rs:87). */
 int jp2g_create(jp2g_ctx** ctx, int device, uint64_t hbm_budget_bytes);
@@ -105,6 +111,18 @@ int jp2g_encode_batch(jp2g_ctx* ctx, const jp2g_request* reqs, uint32_t n, uint8
  * loop. */
 int jp2g_submit(jp2g_ctx* ctx, const jp2g_request* req, uint64_t* ticket);
 int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, int timeout_ms);
+
+/* Cancels a submitted request. JP2G_OK: it had not been admitted to a device
+ * wave, is removed from the queue and its ticket is released (the pixel
+ * buffer may be reused at once; a later jp2g_poll reports an unknown
+ * ticket), or it had already finished (its result is still returned by
+ * jp2g_poll). JP2G_PENDING: its wave is on the device or in Tier-2; the
+ * result is dropped, and jp2g_poll on the ticket returns
+ * JP2G_ENCODE_FAILED ("request cancelled") once the wave is done -- the
+ * pixel buffer must stay valid until then. A poll already waiting on a
+ * cancelled request returns that same status. JP2G_INVALID_INPUT: unknown
+ * ticket. No reference counterpart: the reference has no request queue. */
+int jp2g_cancel(jp2g_ctx* ctx, uint64_t ticket);
 
 /* Tuning knobs (the autotuner sets these):
  * JP2G_OPT_WAVE_BLOCKS        most code-blocks per device wave (default 160000;
@@ -222,7 +240,7 @@ int jp2g_debug_plan(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int
  *
  * d_px: interleaved 8-bit pixels in device memory (w * h * ncomp bytes).
  * d_coef: device buffer of w * h * ncomp int32 that receives the quantised
- * coefficients (the reversible coefficients at quality 100) of each
+ * coefficients (the reversible 5/3 coefficients at any quality >= 100) of each
  * component as a w x h plane in subband (Mallat) layout, component after
  * component -- the same values the full encoder codes.
  * stream: a cudaStream_t (NULL = the legacy default stream). The call only
@@ -236,9 +254,10 @@ int jp2g_debug_plan(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int
  * JP2G_INVALID_INPUT and a message before any device work. All calls share
  * the array, so calls that overlap on the GPU (other streams or threads on
  * the same device) race and must be serialised by the caller. The first call
- * on a device looks up the array's device address for that device; make it
- * before any stream capture. On failure jp2g_last_error(NULL) holds the
- * message. */
+ * on a device looks up the array's device address for that device (and the
+ * first call after the device's context changes, e.g. after
+ * cudaDeviceReset, looks it up again); make that call before any stream
+ * capture. On failure jp2g_last_error(NULL) holds the message. */
 int jp2g_dwt_noalloc(const uint8_t* d_px, uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality,
                      int32_t* d_coef, void* stream);
 

@@ -51,7 +51,7 @@ EXPORTS = [
     "jp2g_last_error", "jp2g_stream", "jp2g_set_timing", "jp2g_stage_times", "jp2g_counters",
     "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
     "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
-    "jp2g_autotune", "jp2g_debug_assemble", "jp2g_debug_plan",
+    "jp2g_autotune", "jp2g_debug_assemble", "jp2g_debug_plan", "jp2g_cancel",
 ]
 
 PENDING = 6
@@ -117,6 +117,7 @@ def load_library(path: str = LIB_PATH):
         lib.jp2g_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]
         lib.jp2g_poll.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(_u8p),
                                   ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]
+        lib.jp2g_cancel.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
         lib.jp2g_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
         lib.jp2g_get_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
         lib.jp2g_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_uint32, ctypes.c_int,
@@ -260,6 +261,19 @@ class Engine:
         data = ctypes.string_at(out, n.value)
         self.lib.jp2g_free(out)
         return data
+
+    def cancel(self, ticket: int) -> bool:
+        """Cancels a submitted page. True: it never reached the device (or
+        had finished) and its pixels are released; False: its wave is in
+        flight, its result is dropped and poll() raises EncodeFailed once
+        the wave is done."""
+        rc = self.lib.jp2g_cancel(self.handle, ticket)
+        if rc == PENDING:
+            return False
+        self._check(rc)
+        with self._inflight_lock:
+            self._inflight.pop(ticket, None)
+        return True
 
     def set_option(self, option: int, value: int):
         self._check(self.lib.jp2g_set_option(self.handle, option, value))

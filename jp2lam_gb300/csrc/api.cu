@@ -78,6 +78,7 @@ struct Ticket {
   uint64_t id = 0;
   PageJob job;
   bool done = false;
+  std::atomic<bool> cancelled{false};  // jp2g_cancel was called: the result is dropped
 };
 
 }  // namespace
@@ -88,6 +89,8 @@ struct jp2g_ctx {
   cudaStream_t stream = nullptr;
   uint64_t budget = 0;
   uint64_t allocated = 0;
+  bool budget_hit = false;         // the last pool growth was refused by the budget
+  uint64_t budget_wave_blocks = 0;  // most code-blocks per wave that fit the budget (0: no cap learnt)
   std::string err;  // guarded by errmu
   std::mutex errmu;
   std::mutex mu;    // device pools and stream: one wave (or encode) at a time
@@ -111,6 +114,7 @@ struct jp2g_ctx {
   std::deque<std::vector<std::shared_ptr<Ticket>>> finishing;
   std::unordered_map<uint64_t, std::shared_ptr<Ticket>> tickets;
   uint64_t next_ticket = 1;
+  int inflight = 0;  // waves taken off `pending` and not yet handed to the finisher
   bool stop = false;
   std::thread worker, finisher;
 };
@@ -142,7 +146,10 @@ bool reserve(jp2g_ctx* c, DevBuf& b, size_t bytes) {
   if (bytes <= b.cap) return true;
   size_t want = std::max(bytes, b.cap + b.cap / 2);
   want = (want + 255) & ~size_t(255);
+  // under a budget, growth beyond the request is dropped before giving up
+  if (c->budget && c->allocated - b.cap + want > c->budget) want = (bytes + 255) & ~size_t(255);
   if (c->budget && c->allocated - b.cap + want > c->budget) {
+    c->budget_hit = true;
     set_msg(c, "device memory budget exhausted (" + std::to_string(c->budget) + " bytes)");
     return false;
   }
@@ -792,6 +799,58 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
   return kOk;
 }
 
+// Frees every device pool (after the stream has drained), so the next wave
+// allocates exactly what it needs under the budget.
+void release_pools(jp2g_ctx* c) {
+  cudaStreamSynchronize(c->stream);
+  DevBuf* bufs[] = {&c->px, &c->ll0, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
+                    &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
+                    &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
+                    &c->itemrec, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases, &c->mqorder,
+                    &c->mqscratch};
+  for (DevBuf* b : bufs) {
+    if (b->p) cudaFree(b->p);
+    b->p = nullptr;
+    b->cap = 0;
+  }
+  c->allocated = 0;
+}
+
+// Admission by the device memory budget: runs a wave, and when a pool could
+// not grow within the budget, releases the pools and runs the two halves of
+// the wave one after the other (recursively), instead of failing its pages.
+// The largest wave that fitted caps later waves (budget_wave_blocks). A single
+// page that does not fit on its own fails alone, with the budget message;
+// the other pages carry on. Counters cover all the parts.
+int run_wave_within_budget(jp2g_ctx* c, PageJob* const* jobs, size_t n, const Prestaged* pre) {
+  c->budget_hit = false;
+  int rc = run_wave(c, jobs, n, nullptr, pre);
+  if (rc == kOk || !c->budget_hit) return rc;
+  // pools sized by earlier waves may crowd out the one this wave needs: try
+  // again from empty pools before splitting
+  release_pools(c);
+  c->budget_hit = false;
+  rc = run_wave(c, jobs, n, nullptr, pre);
+  if (rc == kOk || !c->budget_hit) return rc;
+  const std::string msg = get_msg(c);
+  release_pools(c);
+  uint64_t blocks = 0;
+  for (size_t i = 0; i < n; ++i) blocks += jobs[i]->plan.nblocks;
+  if (n == 1) {
+    jobs[0]->status = kEncodeFailed;
+    jobs[0]->err = msg + ": the page does not fit on its own";
+    return kOk;
+  }
+  c->budget_wave_blocks = std::max<uint64_t>(1, blocks / 2);
+  const size_t h = n / 2;
+  uint64_t counters[8];
+  if ((rc = run_wave_within_budget(c, jobs, h, pre))) return rc;
+  std::memcpy(counters, c->counters, sizeof counters);
+  if ((rc = run_wave_within_budget(c, jobs + h, n - h, pre))) return rc;
+  for (int k = 0; k < 8; ++k) c->counters[k] += counters[k];
+  return kOk;
+}
+
 // Host phase of one page: Tier-2 packet headers, markers and JP2 boxes.
 void finish_page(PageJob* j) {
   if (j->status != kOk) return;
@@ -840,7 +899,14 @@ void read_stage_times(jp2g_ctx* c) {
 // points).
 int encode_one(jp2g_ctx* c, PageJob* j, WaveDebug* dbg) {
   PageJob* jobs[1] = {j};
-  if (int rc = run_wave(c, jobs, 1, dbg, nullptr, true)) return rc;
+  c->budget_hit = false;
+  int rc = run_wave(c, jobs, 1, dbg, nullptr, true);
+  if (rc != kOk && c->budget_hit) {  // pools of earlier waves crowd the budget: retry from empty pools
+    release_pools(c);
+    c->budget_hit = false;
+    rc = run_wave(c, jobs, 1, dbg, nullptr, true);
+  }
+  if (rc) return rc;
   if (j->status != kOk) return set_err(c, j->status, j->err);
   if (dbg && dbg->stop_after_dwt) return kOk;
   finish_page(j);
@@ -860,7 +926,9 @@ constexpr size_t kMaxWavePages = 3000;
 // wave's payload slots stay addressable with 32-bit byte offsets.
 uint64_t wave_block_limit(const jp2g_ctx* c, int cbw) {
   const uint64_t cap = (uint64_t)cbw * (uint64_t)cbw * 4u + 1024u;  // slot_cap of a cbw x cbw block
-  return std::min<uint64_t>((uint64_t)c->opt[JP2G_OPT_WAVE_BLOCKS], 0xffffffffull / cap);
+  uint64_t lim = std::min<uint64_t>((uint64_t)c->opt[JP2G_OPT_WAVE_BLOCKS], 0xffffffffull / cap);
+  if (c->budget_wave_blocks) lim = std::min(lim, c->budget_wave_blocks);
+  return lim;
 }
 
 std::vector<std::vector<PageJob*>> form_waves(jp2g_ctx* c, const std::vector<PageJob*>& jobs) {
@@ -1060,7 +1128,7 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
       });
     }
     const Prestaged pre{bufs[w & 1], staged};
-    rc = run_wave(c, wave.data(), wave.size(), nullptr, &pre);
+    rc = run_wave_within_budget(c, wave.data(), wave.size(), &pre);
     if (stager.joinable()) stager.join();
     staged = next_staged;
     for (int k = 0; k < 8; ++k) counters[k] += c->counters[k];
@@ -1129,6 +1197,7 @@ void worker_loop(jp2g_ctx* c) {
         wave.push_back(c->pending.front());
         c->pending.pop_front();
       }
+      ++c->inflight;
     }
     std::vector<PageJob*> jobs;
     for (auto& t : wave) jobs.push_back(&t->job);
@@ -1136,7 +1205,7 @@ void worker_loop(jp2g_ctx* c) {
     std::string err;
     {
       std::lock_guard<std::mutex> lk(c->mu);
-      rc = run_wave(c, jobs.data(), jobs.size(), nullptr);
+      rc = run_wave_within_budget(c, jobs.data(), jobs.size(), nullptr);
       if (rc != JP2G_OK) err = get_msg(c);
     }
     if (rc != JP2G_OK)
@@ -1147,27 +1216,42 @@ void worker_loop(jp2g_ctx* c) {
     {
       std::lock_guard<std::mutex> lk(c->qmu);
       c->finishing.push_back(std::move(wave));
+      --c->inflight;
     }
     c->fcv.notify_one();
   }
 }
 
 // Finisher: Tier-2 of each finished wave's pages on the host threads, then
-// marks their tickets done.
+// marks their tickets done (a cancelled ticket's result is dropped). It
+// exits once stopping, with nothing queued, no wave on the device (inflight)
+// and nothing left to finish.
 void finisher_loop(jp2g_ctx* c) {
   for (;;) {
     std::vector<std::shared_ptr<Ticket>> wave;
     {
       std::unique_lock<std::mutex> lk(c->qmu);
-      c->fcv.wait(lk, [&] { return !c->finishing.empty() || (c->stop && c->pending.empty()); });
+      c->fcv.wait(lk, [&] {
+        return !c->finishing.empty() || (c->stop && c->pending.empty() && c->inflight == 0);
+      });
       if (c->finishing.empty()) return;
       wave = std::move(c->finishing.front());
       c->finishing.pop_front();
     }
-    parallel_for(wave.size(), host_threads(c), [&](size_t i) { finish_page(&wave[i]->job); });
+    parallel_for(wave.size(), host_threads(c), [&](size_t i) {
+      if (!wave[i]->cancelled) finish_page(&wave[i]->job);
+    });
     {
       std::lock_guard<std::mutex> lk(c->qmu);
-      for (auto& t : wave) t->done = true;
+      for (auto& t : wave) {
+        t->done = true;
+        if (t->cancelled) {
+          t->job.status = kEncodeFailed;
+          t->job.err = "request cancelled";
+          t->job.out.clear();
+          t->job.out.shrink_to_fit();
+        }
+      }
     }
     c->dcv.notify_all();
   }
@@ -1220,6 +1304,29 @@ int jp2g_poll(jp2g_ctx* c, uint64_t ticket, uint8_t** out, size_t* out_len, int 
   // for the whole device phase of a wave) is not needed
   if (t->job.status != JP2G_OK) return set_err(c, t->job.status, t->job.err);
   return finish_output(c, JP2G_OK, t->job.out, out, out_len);
+}
+
+int jp2g_cancel(jp2g_ctx* c, uint64_t ticket) {
+  if (!c) return JP2G_INVALID_INPUT;
+  std::shared_ptr<Ticket> t;
+  {
+    std::lock_guard<std::mutex> lk(c->qmu);
+    auto it = c->tickets.find(ticket);
+    if (it == c->tickets.end()) return set_err(c, JP2G_INVALID_INPUT, "unknown ticket " + std::to_string(ticket));
+    t = it->second;
+    if (t->done) return JP2G_OK;  // finished already: nothing to stop (poll returns the result)
+    t->cancelled = true;
+    auto q = std::find(c->pending.begin(), c->pending.end(), t);
+    if (q == c->pending.end()) return JP2G_PENDING;  // on the device or in Tier-2: the finisher drops the result
+    // not yet admitted to a wave: it never reaches the device
+    c->pending.erase(q);
+    c->tickets.erase(it);
+    t->job.status = kEncodeFailed;
+    t->job.err = "request cancelled";
+    t->done = true;
+  }
+  c->dcv.notify_all();
+  return JP2G_OK;
 }
 
 int jp2g_set_option(jp2g_ctx* c, int option, int64_t value) {

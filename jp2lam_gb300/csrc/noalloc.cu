@@ -35,11 +35,42 @@ namespace {
 constexpr size_t kNoAllocPlaneElems = size_t(1) << 20;
 static __device__ __align__(256) uint32_t g_noalloc_scratch[2 * kNoAllocPlaneElems];
 
-// Host-side address of g_noalloc_scratch per device, resolved once with
-// cudaGetSymbolAddress while that device is current.
+// Host-side address of g_noalloc_scratch per device, resolved with
+// cudaGetSymbolAddress while that device is current, together with the
+// identity of the CUDA context it was resolved in. The address belongs to
+// that context: after cudaDeviceReset (or under another context on the same
+// device) it is resolved again, so a stale address is never launched with.
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 void* g_scratch_ptr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
+
+// Unique id of the calling thread's current CUDA context (0 if none or if
+// the driver does not report one). The driver entry points are fetched
+// through the runtime, so the library does not link libcuda.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+    looked_up = true;
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 __constant__ float kA = -1.586134342059924f;
 __constant__ float kB = -0.052980118572961f;
@@ -229,15 +260,18 @@ extern "C" int jp2g_dwt_noalloc(const uint8_t* d_px, uint32_t w, uint32_t h, uin
     return fail(JP2G_ENCODE_FAILED, "no usable current CUDA device");
   void* scratch = nullptr;
   {
-    // One-time set-up per device: the array's device address, resolved with
-    // the device current. The first call on a device does this, so it should
-    // come before any stream capture that uses this entry point.
+    // Set-up once per device (and again for a new context on it): the
+    // array's device address, resolved with the device current. The first
+    // call on a device does this, so it should come before any stream
+    // capture that uses this entry point.
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_scratch_ptr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
       void* p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // creates the context if needed
       if (e != cudaSuccess || p == nullptr) return fail(JP2G_ENCODE_FAILED, cudaGetErrorString(e));
       g_scratch_ptr[dev] = p;
+      g_scratch_ctx[dev] = current_context_id();
     }
     scratch = g_scratch_ptr[dev];
   }

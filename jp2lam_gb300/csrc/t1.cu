@@ -742,10 +742,11 @@ __device__ __forceinline__ void load_fat_table(uint4* F) {
   }
 }
 
-// Interval/state step of one symbol whose context state index is ci[cx];
-// returns the symbol's C operation (see mq_step for the folded decisions).
+// Interval/state step of one symbol whose context state index is
+// ci[32 * cx] (the calling lane's own copy of the context states); returns
+// the symbol's C operation (see mq_step for the folded decisions).
 __device__ __forceinline__ uint32_t phase_a_one(uint32_t& A, uint32_t* ci, const uint4* F, uint32_t sym) {
-  const uint32_t cx = sym >> 1, cur = ci[cx];
+  const uint32_t cx = sym >> 1, cur = ci[32 * cx];
   const uint4 f = F[cur];
   const uint32_t qe = f.x & 0xffffu;
   const uint32_t lps = ((f.x >> 20) ^ sym) & 1u;
@@ -753,7 +754,7 @@ __device__ __forceinline__ uint32_t phase_a_one(uint32_t& A, uint32_t* ci, const
   const bool take_a = (a < qe) == (lps != 0);
   const uint32_t n = take_a ? ((a < 0x4000u ? 1u : 0u) + (a < 0x8000u ? 1u : 0u)) : ((f.x >> 16) & 15u);
   A = (take_a ? a : qe) << n;
-  ci[cx] = n ? (lps ? (f.w >> 8) : (f.w & 0xffu)) : cur;
+  ci[32 * cx] = n ? (lps ? (f.w >> 8) : (f.w & 0xffu)) : cur;
   return (take_a ? qe : 0u) | (n << 16);
 }
 
@@ -765,15 +766,15 @@ __device__ __forceinline__ void phase_a_chunk(uint32_t& A, uint32_t* ci, const u
   uint32_t sy[16];
   #pragma unroll
   for (int i = 0; i < 16; ++i) sy[i] = chunk_sym(q, i);
-  uint32_t cur = ci[sy[0] >> 1];
+  uint32_t cur = ci[32 * (sy[0] >> 1)];
   uint4 f = F[cur];
-  uint32_t idx_next = ci[sy[1] >> 1];
+  uint32_t idx_next = ci[32 * (sy[1] >> 1)];
   uint4 fl_next = F[idx_next];
   #pragma unroll
   for (int i = 0; i < 16; ++i) {
     const uint32_t cx = sy[i] >> 1;
     uint32_t raw2 = 0;
-    if (i + 2 < 16) raw2 = ci[sy[i + 2] >> 1];  // before this symbol's update
+    if (i + 2 < 16) raw2 = ci[32 * (sy[i + 2] >> 1)];  // before this symbol's update
     const uint32_t qe = f.x & 0xffffu;
     const uint32_t lps = ((f.x >> 20) ^ sy[i]) & 1u;
     const uint32_t a = A - qe;
@@ -783,7 +784,7 @@ __device__ __forceinline__ void phase_a_chunk(uint32_t& A, uint32_t* ci, const u
     op[i] = (take_a ? qe : 0u) | (n << 16);
     const uint32_t newidx = n ? (lps ? (f.w >> 8) : (f.w & 0xffu)) : cur;
     const uint32_t newx = n ? (lps ? f.z : f.y) : f.x;
-    ci[cx] = newidx;
+    ci[32 * cx] = newidx;
     if (i + 1 < 16) {
       const uint4 L = F[newidx];
       const uint32_t cxn = sy[i + 1] >> 1;
@@ -833,7 +834,12 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
   constexpr int HL = 32 / H;  // lanes per chain
   __shared__ uint4 F[94];
   __shared__ PipeChunk slots[kPipes][2][H];
-  __shared__ uint32_t ci_all[kPipes][H][20];
+  // Context state indices: every lane keeps its own copy (context c of a
+  // lane at [pipe][c][lane]). The lanes of a chain compute identical values,
+  // but a shared copy would be read and written by all of them with nothing
+  // ordering one lane's write after another lane's read of the same symbol;
+  // private copies make the chain correct however the lanes are scheduled.
+  __shared__ uint32_t ci_all[kPipes][19][32];
   if (blockIdx.x >= pipe_ctas) {
     __shared__ uint2 T[94];
     __shared__ uint2 ce_all[kPipes * 2][20 * 32];
@@ -855,7 +861,7 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
   const int bar = 1 + pipe;
   if (warp < kPipes) {
     // ---- producer: interval and state chain ----
-    uint32_t* ci = ci_all[pipe][half];
+    uint32_t* ci = &ci_all[pipe][0][lane];
     uint32_t b = kPipeEnd, base = 0, A = 0x8000u;
     int mbp = 0, j = 0, lo = 0, total = 0;
     bool exhausted = false;  // the block queue is empty for this chain
@@ -891,8 +897,8 @@ __global__ void __launch_bounds__(kPipes * 64, 2) t1_mq_pipe_kernel(T1Args a, ui
         base = a.plane_base[b];
         A = 0x8000u;
         // contexts: state 0 except UNI 46, AGG 3, ZC 4 (src/mq/mod.rs:195-200)
-        for (int x = hl; x < 19; x += HL) ci[x] = x == kCtxUNI ? 92u : (x == kCtxAGG ? 6u : (x == 0 ? 8u : 0u));
-        __syncwarp(hmask);
+        #pragma unroll
+        for (int x = 0; x < 19; ++x) ci[32 * x] = x == kCtxUNI ? 92u : (x == kCtxAGG ? 6u : (x == 0 ? 8u : 0u));
         flags = 1;
         start_item();
       }

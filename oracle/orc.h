@@ -152,6 +152,17 @@ std::vector<Layout> tier1_layouts(const Plan& p, const Planes& px,
 
 // Tier-2 / codestream / JP2 (host side in the reference).
 std::vector<uint8_t> build_payload(const std::vector<Layout>& layouts);
+// One tile-part of a codestream as the writer frames it.
+struct TilePartBytes {
+  uint16_t tile_index = 0;
+  uint8_t part_index = 0, total_parts = 0;
+  std::vector<std::vector<uint8_t>> header_segments;
+  std::vector<uint8_t> payload;
+};
+std::vector<uint8_t> frame_codestream(const Plan& p, const std::vector<std::vector<uint8_t>>& main_segments,
+                                      const std::vector<TilePartBytes>& parts);
+bool parse_single_tile(const uint8_t* b, size_t n, std::vector<std::vector<uint8_t>>* main_segments,
+                       TilePartBytes* tp);
 std::vector<uint8_t> build_codestream(const Plan& p,
                                       const std::vector<uint8_t>& payload);
 std::vector<uint8_t> wrap_jp2(const Plan& p, const std::vector<uint8_t>& cs);
@@ -168,7 +179,7 @@ struct Decoded {
   int ncomp;
   Planes comps;
 };
-Decoded decode(const uint8_t* bytes, size_t n);
+Decoded decode(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane = false);
 
 // Quality metrics as encode_with_psnr defines them.
 void quality_metrics(const Plan& p, const Planes& px, const EncodeOptions& opt,

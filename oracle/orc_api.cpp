@@ -76,6 +76,66 @@ int orc_assemble(uint32_t w, uint32_t h, int ncomp, int quality, int format, con
   }
 }
 
+// Codestream framing alone (src/j2k/write.rs:9-113) under the plan of a
+// w x h x ncomp page at `quality`: SOC, the main-header segments in `main`
+// (marker segments back to back, split by their length fields), one
+// tile-part (tile, part, parts) with the header segments in `tile_hdr` and
+// the payload bytes, EOC.
+int orc_frame(uint32_t w, uint32_t h, int ncomp, int quality, const uint8_t* main, size_t main_n,
+              const uint8_t* tile_hdr, size_t tile_hdr_n, int tile, int part, int parts,
+              const uint8_t* payload, size_t payload_n, uint8_t** out, size_t* out_len) {
+  if (int rc = check_input(w, h, ncomp)) return rc;
+  auto split = [](const uint8_t* b, size_t n, std::vector<std::vector<uint8_t>>* segs) {
+    size_t i = 0;
+    while (i + 4 <= n) {
+      const size_t len = 2 + ((size_t)b[i + 2] << 8 | b[i + 3]);
+      if (i + len > n) return false;
+      segs->emplace_back(b + i, b + i + len);
+      i += len;
+    }
+    return i == n;
+  };
+  try {
+    orc::Plan p = orc::build_plan(w, h, ncomp, quality, 0);
+    std::vector<std::vector<uint8_t>> segs;
+    orc::TilePartBytes tp;
+    if (!split(main, main_n, &segs) || !split(tile_hdr, tile_hdr_n, &tp.header_segments)) {
+      g_err = "malformed marker segments";
+      return orc::kInvalidInput;
+    }
+    tp.tile_index = (uint16_t)tile;
+    tp.part_index = (uint8_t)part;
+    tp.total_parts = (uint8_t)parts;
+    tp.payload.assign(payload, payload + payload_n);
+    *out = dup(orc::frame_codestream(p, segs, {tp}), out_len);
+    return 0;
+  } catch (const orc::Error& e) {
+    return fail(e);
+  }
+}
+
+// Parses a single-tile codestream into its parts and frames it again under
+// the plan of a w x h x ncomp page at `quality`
+// (CodestreamParts::parse_single_tile + encode, src/j2k/parse.rs,
+// src/j2k/write.rs).
+int orc_reframe(const uint8_t* cs, size_t n, uint32_t w, uint32_t h, int ncomp, int quality, uint8_t** out,
+                size_t* out_len) {
+  if (int rc = check_input(w, h, ncomp)) return rc;
+  try {
+    orc::Plan p = orc::build_plan(w, h, ncomp, quality, 0);
+    std::vector<std::vector<uint8_t>> segs;
+    orc::TilePartBytes tp;
+    if (!orc::parse_single_tile(cs, n, &segs, &tp)) {
+      g_err = "not a single-tile codestream";
+      return orc::kDecodeFailed;
+    }
+    *out = dup(orc::frame_codestream(p, segs, {tp}), out_len);
+    return 0;
+  } catch (const orc::Error& e) {
+    return fail(e);
+  }
+}
+
 // Quantised coefficient plane of one component (Mallat layout, W*H int32).
 int orc_coefficients(const uint8_t* px, uint32_t w, uint32_t h, int ncomp,
                      int quality, int comp, int32_t* out) {
@@ -212,10 +272,12 @@ int orc_block_summary(const uint8_t* px, uint32_t w, uint32_t h, int ncomp,
 }
 
 // Decode J2K/JP2 bytes -> interleaved 8-bit pixels (caller buffer W*H*C).
-int orc_decode(const uint8_t* bytes, size_t n, uint32_t* w, uint32_t* h, int* ncomp,
-               uint8_t* px, size_t cap) {
+// The same, optionally reading RCT chroma code-blocks with the extra
+// bit-plane their encoder used (the reference's decoder does not).
+int orc_decode_ex(const uint8_t* bytes, size_t n, int rct_chroma_extra_bitplane, uint32_t* w, uint32_t* h,
+                  int* ncomp, uint8_t* px, size_t cap) {
   try {
-    orc::Decoded d = orc::decode(bytes, n);
+    orc::Decoded d = orc::decode(bytes, n, rct_chroma_extra_bitplane != 0);
     *w = d.width;
     *h = d.height;
     *ncomp = d.ncomp;
@@ -227,6 +289,11 @@ int orc_decode(const uint8_t* bytes, size_t n, uint32_t* w, uint32_t* h, int* nc
   } catch (const orc::Error& e) {
     return fail(e);
   }
+}
+
+int orc_decode(const uint8_t* bytes, size_t n, uint32_t* w, uint32_t* h, int* ncomp,
+               uint8_t* px, size_t cap) {
+  return orc_decode_ex(bytes, n, 0, w, h, ncomp, px, cap);
 }
 
 int orc_quality_metrics(const uint8_t* px, uint32_t w, uint32_t h, int ncomp,

@@ -506,11 +506,10 @@ std::vector<uint8_t> build_payload(const std::vector<Layout>& layouts) {
 static void be16(std::vector<uint8_t>& o, uint32_t v) { o.push_back((uint8_t)(v >> 8)); o.push_back((uint8_t)v); }
 static void be32(std::vector<uint8_t>& o, uint32_t v) { be16(o, v >> 16); be16(o, v & 0xffff); }
 
-std::vector<uint8_t> build_codestream(const Plan& p, const std::vector<uint8_t>& payload) {
-  // src/j2k/markers.rs:8-110 and src/j2k/write.rs:9-77
+// SIZ, COD and QCD marker segments of a plan (src/j2k/markers.rs:8-110).
+static std::vector<uint8_t> siz_segment(const Plan& p) {
   std::vector<uint8_t> o;
-  be16(o, 0xff4f);
-  be16(o, 0xff51);  // SIZ
+  be16(o, 0xff51);
   be16(o, 38 + 3 * p.ncomp);
   be16(o, 0);
   be32(o, p.width); be32(o, p.height);
@@ -523,7 +522,12 @@ std::vector<uint8_t> build_codestream(const Plan& p, const std::vector<uint8_t>&
     o.push_back(1);
     o.push_back(1);
   }
-  be16(o, 0xff52);  // COD
+  return o;
+}
+
+static std::vector<uint8_t> cod_segment(const Plan& p) {
+  std::vector<uint8_t> o;
+  be16(o, 0xff52);
   be16(o, 12);
   o.push_back(0);
   o.push_back(0);  // LRCP
@@ -534,7 +538,12 @@ std::vector<uint8_t> build_codestream(const Plan& p, const std::vector<uint8_t>&
   o.push_back((uint8_t)(__builtin_ctz(p.cbh) - 2));
   o.push_back(0);
   o.push_back(p.lossless ? 1 : 0);
-  be16(o, 0xff5c);  // QCD
+  return o;
+}
+
+static std::vector<uint8_t> qcd_segment(const Plan& p) {
+  std::vector<uint8_t> o;
+  be16(o, 0xff5c);
   if (p.lossless) {
     be16(o, 3 + (uint32_t)p.quants.size());
     o.push_back((uint8_t)(p.guard_bits << 5));
@@ -544,18 +553,90 @@ std::vector<uint8_t> build_codestream(const Plan& p, const std::vector<uint8_t>&
     o.push_back((uint8_t)((p.guard_bits << 5) | 2));
     for (const auto& q : p.quants) be16(o, ((uint32_t)(q.exponent & 0xff) << 11 | (q.mantissa & 0x7ff)) & 0xffff);
   }
-  be16(o, 0xff90);  // SOT
-  be16(o, 10);
-  be16(o, 0);
-  uint64_t psot = 12 + 2 + (uint64_t)payload.size();
-  if (psot > 0xffffffffull) throw Error(kEncodeFailed, "tile-part length exceeds Psot range");
-  be32(o, (uint32_t)psot);
-  o.push_back(0);
-  o.push_back(1);
-  be16(o, 0xff93);
-  o.insert(o.end(), payload.begin(), payload.end());
+  return o;
+}
+
+// A main-header segment as the writer emits it: SIZ and COD are re-encoded
+// from the plan when the plan's segment has the same length, QCD only for a
+// reversible plan, anything else passes through (src/j2k/write.rs:80-113).
+static void put_main_segment(std::vector<uint8_t>& o, const std::vector<uint8_t>& seg, const Plan& p) {
+  const uint32_t m = seg.size() >= 2 ? ((uint32_t)seg[0] << 8 | seg[1]) : 0u;
+  std::vector<uint8_t> local;
+  if (m == 0xff51) local = siz_segment(p);
+  else if (m == 0xff52) local = cod_segment(p);
+  else if (m == 0xff5c && p.lossless) local = qcd_segment(p);
+  const std::vector<uint8_t>& use = !local.empty() && local.size() == seg.size() ? local : seg;
+  for (uint8_t b : use) o.push_back(b);
+}
+
+// Codestream framing (CodestreamParts::encode, src/j2k/write.rs:9-77): SOC,
+// the main-header segments, then per tile-part an SOT segment (Lsot 10,
+// Isot, Psot = 12 + header segments + 2 + payload, TPsot, TNsot), its header
+// segments, SOD and its payload; EOC.
+std::vector<uint8_t> frame_codestream(const Plan& p, const std::vector<std::vector<uint8_t>>& main_segments,
+                                      const std::vector<TilePartBytes>& parts) {
+  if (p.ncomp == 0) throw Error(kEncodeFailed, "cannot emit codestream with zero components");
+  std::vector<uint8_t> o;
+  be16(o, 0xff4f);
+  for (const auto& seg : main_segments) put_main_segment(o, seg, p);
+  for (const auto& tp : parts) {
+    uint64_t psot = 12 + 2 + (uint64_t)tp.payload.size();
+    for (const auto& h : tp.header_segments) psot += h.size();
+    if (psot > 0xffffffffull) throw Error(kEncodeFailed, "tile-part length exceeds Psot range");
+    be16(o, 0xff90);
+    be16(o, 10);
+    be16(o, tp.tile_index);
+    be32(o, (uint32_t)psot);
+    o.push_back(tp.part_index);
+    o.push_back(tp.total_parts);
+    for (const auto& h : tp.header_segments) o.insert(o.end(), h.begin(), h.end());
+    be16(o, 0xff93);
+    o.insert(o.end(), tp.payload.begin(), tp.payload.end());
+  }
   be16(o, 0xffd9);
   return o;
+}
+
+// Splits a single-tile codestream into its main-header segments and one
+// tile-part (CodestreamParts::parse_single_tile, src/j2k/parse.rs): marker
+// segments are delimited by their length fields; the payload runs from SOD
+// to the EOC that ends the stream.
+bool parse_single_tile(const uint8_t* b, size_t n, std::vector<std::vector<uint8_t>>* main_segments,
+                       TilePartBytes* tp) {
+  auto u16 = [&](size_t i) { return (uint32_t)b[i] << 8 | b[i + 1]; };
+  if (n < 4 || u16(0) != 0xff4f || u16(n - 2) != 0xffd9) return false;
+  size_t i = 2;
+  while (i + 4 <= n && u16(i) != 0xff90) {
+    const size_t len = 2 + u16(i + 2);
+    if (i + len > n) return false;
+    main_segments->emplace_back(b + i, b + i + len);
+    i += len;
+  }
+  if (i + 12 > n || u16(i) != 0xff90 || u16(i + 2) != 10) return false;
+  tp->tile_index = (uint16_t)u16(i + 4);
+  tp->part_index = b[i + 10];
+  tp->total_parts = b[i + 11];
+  i += 12;
+  while (i + 2 <= n && u16(i) != 0xff93) {
+    if (i + 4 > n) return false;
+    const size_t len = 2 + u16(i + 2);
+    if (i + len > n) return false;
+    tp->header_segments.emplace_back(b + i, b + i + len);
+    i += len;
+  }
+  if (i + 2 > n - 2) return false;
+  tp->payload.assign(b + i + 2, b + n - 2);
+  return true;
+}
+
+std::vector<uint8_t> build_codestream(const Plan& p, const std::vector<uint8_t>& payload) {
+  // the encoder's one tile-part: tile 0, part 0 of 1 (backend.rs:275-290)
+  TilePartBytes tp;
+  tp.tile_index = 0;
+  tp.part_index = 0;
+  tp.total_parts = 1;
+  tp.payload = payload;
+  return frame_codestream(p, {siz_segment(p), cod_segment(p), qcd_segment(p)}, {tp});
 }
 
 std::vector<uint8_t> wrap_jp2(const Plan& p, const std::vector<uint8_t>& cs) {
@@ -654,7 +735,7 @@ struct DTagTree {
 };
 }  // namespace
 
-Decoded decode(const uint8_t* bytes, size_t n) {
+Decoded decode(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane) {
 
   const uint8_t* cs = bytes;
   size_t csn = n;
@@ -784,7 +865,10 @@ Decoded decode(const uint8_t* bytes, size_t n) {
         const auto& rc = rects[b.bi];
         if (body + b.len > payload_end) throw Error(kDecodeFailed, "code-block data past tile-part end");
         size_t si = b.bi % steps.size();
-        int mb = guard - 1 + steps[si].first;
+        // Mb from QCD as the reference's decoder takes it (decode/t1.rs:56);
+        // optionally with the extra bit-plane the encoder gives RCT chroma
+        // at q >= 100 (backend.rs:179-189), which QCD does not signal
+        int mb = guard - 1 + steps[si].first + (rct_chroma_extra_bitplane && rev && mct && comp > 0 ? 1 : 0);
         int bw = b.x1 - b.x0, bh = b.y1 - b.y0;
         auto dv = decode_block(cs + body, b.len, bw, bh, rc.band, mb, b.zbp, b.np);
         for (int y = 0; y < bh; ++y)

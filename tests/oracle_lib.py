@@ -148,17 +148,48 @@ class Oracle:
         self._err(rc, "orc_block_summary")
         return rows[:9 * n.value].reshape(-1, 9)
 
-    def decode(self, data):
+    def decode(self, data, rct_chroma_extra_bitplane=False):
+        """The reference's decoder (src/decode/*.rs); with
+        rct_chroma_extra_bitplane, RCT chroma code-blocks are read with the
+        extra bit-plane their encoder gave them (backend.rs:179-189), which
+        the reference's decoder does not do."""
         w, h, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int()
-        rc = self.lib.orc_decode(data, ctypes.c_size_t(len(data)), ctypes.byref(w), ctypes.byref(h),
-                                 ctypes.byref(c), None, ctypes.c_size_t(0))
+        flag = int(bool(rct_chroma_extra_bitplane))
+        rc = self.lib.orc_decode_ex(data, ctypes.c_size_t(len(data)), flag, ctypes.byref(w), ctypes.byref(h),
+                                    ctypes.byref(c), None, ctypes.c_size_t(0))
         self._err(rc, "orc_decode")
         px = np.zeros(w.value * h.value * c.value, np.uint8)
-        rc = self.lib.orc_decode(data, ctypes.c_size_t(len(data)), ctypes.byref(w), ctypes.byref(h),
-                                 ctypes.byref(c), px.ctypes.data_as(ctypes.c_void_p),
-                                 ctypes.c_size_t(px.size))
+        rc = self.lib.orc_decode_ex(data, ctypes.c_size_t(len(data)), flag, ctypes.byref(w), ctypes.byref(h),
+                                    ctypes.byref(c), px.ctypes.data_as(ctypes.c_void_p),
+                                    ctypes.c_size_t(px.size))
         self._err(rc, "orc_decode")
         return w.value, h.value, c.value, px
+
+    def frame(self, w, h, ncomp, quality, main, tile_hdr, payload, tile=0, part=0, parts=0):
+        """Codestream framing alone (src/j2k/write.rs:9-113): SOC, the
+        main-header segments `main`, one tile-part with header segments
+        `tile_hdr` and `payload`, EOC; under the plan of a w x h page."""
+        out = _u8p()
+        n = ctypes.c_size_t()
+        rc = self.lib.orc_frame(ctypes.c_uint32(w), ctypes.c_uint32(h), ncomp, quality, bytes(main),
+                                ctypes.c_size_t(len(main)), bytes(tile_hdr), ctypes.c_size_t(len(tile_hdr)),
+                                tile, part, parts, bytes(payload), ctypes.c_size_t(len(payload)),
+                                ctypes.byref(out), ctypes.byref(n))
+        self._err(rc, "orc_frame")
+        data = ctypes.string_at(out, n.value)
+        self.lib.orc_free(out)
+        return data
+
+    def reframe(self, cs, w, h, ncomp, quality):
+        """Parses a single-tile codestream and frames it again."""
+        out = _u8p()
+        n = ctypes.c_size_t()
+        rc = self.lib.orc_reframe(bytes(cs), ctypes.c_size_t(len(cs)), ctypes.c_uint32(w), ctypes.c_uint32(h),
+                                  ncomp, quality, ctypes.byref(out), ctypes.byref(n))
+        self._err(rc, "orc_reframe")
+        data = ctypes.string_at(out, n.value)
+        self.lib.orc_free(out)
+        return data
 
     def quality_metrics(self, px, w, h, ncomp, quality):
         px = np.ascontiguousarray(px, dtype=np.uint8)

@@ -440,16 +440,51 @@ def test_gray_lossless_jp2_roundtrip(orc):
     assert np.array_equal(dec, px)
 
 
-def test_codestream_framing(orc):
-    """j2k/mod.rs:80-133: SOC first, SOT with Psot = 12 + 2 + payload,
-    SOD, EOC last."""
+# The reference's literal codestream-writer vectors (src/j2k/mod.rs:44-133),
+# under the plan of a 1x1 gray page at Preset::DocumentHigh's quality (the
+# plan only matters for SIZ/COD/QCD segments of its own lengths, which these
+# opaque segments are not). The oracle's encoder frames every codestream
+# with this same writer (build_codestream -> frame_codestream).
+_DOCUMENT_HIGH = 85  # Preset::DocumentHigh.quality() (src/model.rs:54-61)
+_LITERAL_PARSED = bytes([
+    0xff, 0x4f, 0xff, 0x51, 0x00, 0x04, 0x12, 0x34, 0xff, 0x52, 0x00, 0x05, 0xaa, 0xbb,
+    0xcc, 0xff, 0x90, 0x00, 0x0a, 0x00, 0x00, 0x00, 0x00, 0x00, 0x17, 0x00, 0x00, 0xff,
+    0x64, 0x00, 0x03, 0x01, 0xff, 0x93, 0xde, 0xad, 0xbe, 0xef, 0xff, 0xd9,
+])
+_LITERAL_WRITTEN = bytes([
+    0xff, 0x4f, 0xff, 0x51, 0x00, 0x04, 0x12, 0x34, 0xff, 0x52, 0x00, 0x05, 0xaa, 0xbb,
+    0xcc, 0xff, 0x90, 0x00, 0x0a, 0x00, 0x00, 0x00, 0x00, 0x00, 0x18, 0x00, 0x00, 0xff,
+    0x64, 0x00, 0x03, 0x01, 0xff, 0x93, 0x10, 0x20, 0x30, 0x40, 0x50, 0xff, 0xd9,
+])
+
+
+def test_parser_reemits_single_tile_codestream(orc):
+    """j2k/mod.rs:44-76: parse a single-tile codestream and write it again."""
+    assert orc.reframe(_LITERAL_PARSED, 1, 1, 1, _DOCUMENT_HIGH) == _LITERAL_PARSED
+
+
+def test_writer_accepts_locally_constructed_packet_sequence(orc):
+    """j2k/mod.rs:78-133: two opaque main-header segments, one tile-part
+    (tile 0, part 0, 0 parts) with a COM segment and a payload of a
+    header+body packet (10 20 | 30) and an opaque packet (40 50)."""
+    main = bytes([0xff, 0x51, 0x00, 0x04, 0x12, 0x34, 0xff, 0x52, 0x00, 0x05, 0xaa, 0xbb, 0xcc])
+    tile_hdr = bytes([0xff, 0x64, 0x00, 0x03, 0x01])
+    payload = bytes([0x10, 0x20, 0x30, 0x40, 0x50])
+    assert orc.frame(1, 1, 1, _DOCUMENT_HIGH, main, tile_hdr, payload, 0, 0, 0) == _LITERAL_WRITTEN
+
+
+def test_encoder_codestream_is_the_writer_framing(orc):
+    """An encoded codestream re-frames to itself: its SIZ/COD/QCD are the
+    plan's own segments and its SOT carries tile 0, part 0 of 1 with
+    Psot = 12 + 2 + payload (backend.rs:275-290)."""
     px = np.arange(64, dtype=np.uint8)
-    cs = orc.encode(px, 8, 8, 1, 85, fmt=0)
-    assert cs[:2] == b"\xff\x4f" and cs[-2:] == b"\xff\xd9"
-    sot = cs.index(b"\xff\x90")
-    psot = int.from_bytes(cs[sot + 6:sot + 10], "big")
-    assert sot + psot == len(cs) - 2
-    assert cs[sot + 12:sot + 14] == b"\xff\x93"
+    for q in (85, 100):
+        cs = orc.encode(px, 8, 8, 1, q, fmt=0)
+        assert orc.reframe(cs, 8, 8, 1, q) == cs
+        sot = cs.index(b"\xff\x90")
+        psot = int.from_bytes(cs[sot + 6:sot + 10], "big")
+        assert sot + psot == len(cs) - 2
+        assert cs[sot + 10:sot + 14] == b"\x00\x01\xff\x93"
 
 
 def test_synthetic_rgb_quality_sweep_is_valid_jp2(orc):
@@ -490,3 +525,24 @@ def test_lossy_decode_psnr_near_encoder_estimate(orc):
     psnr_est, ssim = orc.quality_metrics(px, w, h, 1, 75)
     assert psnr_dec > 20.0 and 0.0 < ssim <= 1.0
     assert abs(psnr_dec - psnr_est) < 2.0
+
+
+def test_rgb_lossless_chroma_needs_the_extra_bitplane_to_decode(orc):
+    """At q >= 100 with RCT the encoder codes chroma with precision + 1
+    (backend.rs:179-189) while QCD carries component 0's exponents
+    (plan/mod.rs:141-145); the reference's decoder takes Mb from QCD
+    (decode/t1.rs:56) and rejects more passes than 1 + 3 (Mb - 1)
+    (decode/t1.rs:121-126). So its own sRGB lossless output does not decode
+    with its own decoder, and reads back exactly once chroma is given the
+    extra bit-plane. Byte identity with the reference stays the parity mode."""
+    for w, h in ((64, 64), (7, 3), (333, 211)):
+        y, x = np.mgrid[0:h, 0:w]
+        px = np.stack([(x * 5 + y) & 255, (y * 3) & 255, ((x ^ y) * 7) & 255], -1).astype(np.uint8).ravel()
+        data = orc.encode(px, w, h, 3, 100, fmt=1)
+        with pytest.raises(RuntimeError, match="pass count exceeds maximum"):
+            orc.decode(data)
+        dw, dh, dc, dec = orc.decode(data, rct_chroma_extra_bitplane=True)
+        assert (dw, dh, dc) == (w, h, 3)
+        assert np.array_equal(dec, px)
+    gray = np.arange(64 * 64, dtype=np.uint32).astype(np.uint8)
+    assert np.array_equal(orc.decode(orc.encode(gray, 64, 64, 1, 100, fmt=1))[3], gray)
