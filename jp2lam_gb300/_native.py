@@ -263,10 +263,10 @@ class Engine:
         return data
 
     def cancel(self, ticket: int) -> bool:
-        """Cancels a submitted page. True: it never reached the device (or
-        had finished) and its pixels are released; False: its wave is in
-        flight, its result is dropped and poll() raises EncodeFailed once
-        the wave is done."""
+        """Cancels a submitted page. True: it never reached the device, or
+        it had finished and its result is dropped; its ticket and pixels are
+        released. False: its wave is in flight, its result is dropped and
+        poll() raises EncodeFailed once the wave is done."""
         rc = self.lib.jp2g_cancel(self.handle, ticket)
         if rc == PENDING:
             return False

@@ -1314,7 +1314,10 @@ int jp2g_cancel(jp2g_ctx* c, uint64_t ticket) {
     auto it = c->tickets.find(ticket);
     if (it == c->tickets.end()) return set_err(c, JP2G_INVALID_INPUT, "unknown ticket " + std::to_string(ticket));
     t = it->second;
-    if (t->done) return JP2G_OK;  // finished already: nothing to stop (poll returns the result)
+    if (t->done) {  // finished already: the result is dropped with the ticket
+      c->tickets.erase(it);
+      return JP2G_OK;
+    }
     t->cancelled = true;
     auto q = std::find(c->pending.begin(), c->pending.end(), t);
     if (q == c->pending.end()) return JP2G_PENDING;  // on the device or in Tier-2: the finisher drops the result
