@@ -261,6 +261,13 @@ int jp2g_debug_plan(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int
 int jp2g_dwt_noalloc(const uint8_t* d_px, uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality,
                      int32_t* d_coef, void* stream);
 
+/* Host-only, no device needed: the bit-sliced context formation the
+ * modelling kernel uses (zero-coding labels of 64 samples per logic
+ * operation, sign contexts and prediction bits), evaluated on single samples
+ * for every neighbourhood, in the layout of jp2g_tables' zc, sc and spb, so
+ * a test can compare it with the tables entry for entry. */
+void jp2g_debug_context_labels(uint8_t* zc, uint8_t* sc, uint8_t* spb);
+
 /* Host-only, no device needed: the Tier-1 context tables (zero coding
  * 4x512, sign context 256, sign prediction 256) and the MQ state table
  * (94 entries, qe | next_mps << 16 | next_lps << 24) the kernels use. */

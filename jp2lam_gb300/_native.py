@@ -51,7 +51,7 @@ EXPORTS = [
     "jp2g_last_error", "jp2g_stream", "jp2g_set_timing", "jp2g_stage_times", "jp2g_counters",
     "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
     "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
-    "jp2g_autotune", "jp2g_debug_assemble", "jp2g_debug_plan", "jp2g_cancel",
+    "jp2g_autotune", "jp2g_debug_assemble", "jp2g_debug_plan", "jp2g_cancel", "jp2g_debug_context_labels",
 ]
 
 PENDING = 6
@@ -335,6 +335,17 @@ class Engine:
                                                quality, rows.ctypes.data_as(ctypes.c_void_p), n.value,
                                                ctypes.byref(n)))
         return rows.reshape(-1, 8)
+
+
+def context_labels():
+    """The bit-sliced context formation evaluated on single samples, in the
+    layout of tables() (zc, sc, spb)."""
+    lib = load_library()
+    zc = np.zeros(2048, np.uint8)
+    sc = np.zeros(256, np.uint8)
+    spb = np.zeros(256, np.uint8)
+    lib.jp2g_debug_context_labels(*(a.ctypes.data_as(ctypes.c_void_p) for a in (zc, sc, spb)))
+    return zc, sc, spb
 
 
 def tables():

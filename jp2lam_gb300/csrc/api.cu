@@ -32,6 +32,7 @@ void build_t1_tables(uint8_t* zc, uint8_t* sc, uint8_t* spb, uint32_t* mq);
 bool assemble_codestream(const PagePlan& p, const BlockKeep* keep, const uint8_t* body,
                          const uint32_t* offsets, std::vector<uint8_t>* out, Failure* err);
 double norm97(int level, int orient);
+void context_labels_from_logic(uint8_t* zc, uint8_t* sc, uint8_t* spb);
 }  // namespace jp2g
 
 using namespace jp2g;
@@ -1623,6 +1624,10 @@ int jp2g_debug_plan(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int
 
 // Host-only: the Tier-1 tables the device uses, for checking against the
 // reference's literal tables without a GPU.
+void jp2g_debug_context_labels(uint8_t* zc, uint8_t* sc, uint8_t* spb) {
+  jp2g::context_labels_from_logic(zc, sc, spb);
+}
+
 void jp2g_tables(uint8_t* zc, uint8_t* sc, uint8_t* spb, uint32_t* mq) {
   build_t1_tables(zc, sc, spb, mq);
 }

@@ -31,6 +31,7 @@
 
 #include "jp2g_internal.h"
 #include "kernels.h"
+#include "t1_logic.h"
 
 namespace jp2g {
 
@@ -38,7 +39,7 @@ namespace {
 
 // Context numbers (src/mq/mod.rs:5-10).
 constexpr int kCtxAGG = 17, kCtxUNI = 18;
-constexpr int kModelWarps = 8;
+constexpr int kModelWarps = 4;  // 7 KB of shared memory each: 6 CTAs per SM
 constexpr int kMqWarps = 4;
 
 struct Tables {
@@ -50,10 +51,6 @@ struct Tables {
 
 // Built on the host from the standard's rules, copied in by upload_t1_tables.
 __constant__ Tables c_tables;
-
-__device__ __forceinline__ uint64_t westm(uint64_t m) { return m << 1; }   // bit x = m[x-1]
-__device__ __forceinline__ uint64_t eastm(uint64_t m) { return m >> 1; }   // bit x = m[x+1]
-__device__ __forceinline__ uint64_t dil(uint64_t m) { return m | (m << 1) | (m >> 1); }
 
 // ---------------------------------------------------------------- analyze --
 __global__ void t1_analyze_kernel(T1Args a) {
@@ -97,70 +94,106 @@ __global__ void t1_items_kernel(T1Args a) {
 }
 
 // ------------------------------------------------------------------ model --
+// Modelling works on the code-block in column layout: lane L owns columns
+// L ("A") and L + 32 ("B"), and every per-sample state of a column is a
+// 64-bit mask with bit y = row y. Vertical neighbours are then shifts of the
+// lane's own masks, horizontal ones a shuffle from the adjacent lane, and one
+// logic operation handles 64 samples.
+constexpr uint64_t kRow0 = 0x1111111111111111ull;  // first row of each stripe
+constexpr uint64_t kRow3 = 0x8888888888888888ull;  // last row of each stripe
+
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
+  const uint32_t lo = __shfl_sync(~0u, (uint32_t)v, src);
+  const uint32_t hi = __shfl_sync(~0u, (uint32_t)(v >> 32), src);
+  return (uint64_t)hi << 32 | lo;
+}
+
+// The masks of the columns west and east of this lane's columns A and B.
+struct Side {
+  uint64_t wa, ea, wb, eb;
+};
+__device__ __forceinline__ Side sides(uint64_t a, uint64_t b, int lane) {
+  const int up = (lane + 31) & 31, dn = (lane + 1) & 31;
+  Side r;
+  r.wa = shfl64(a, up);                   // column L - 1 (none for lane 0)
+  r.wb = shfl64(lane == 31 ? a : b, up);  // column L + 31 (lane 0: column 31)
+  r.ea = shfl64(lane == 0 ? b : a, dn);   // column L + 1 (lane 31: column 32)
+  r.eb = shfl64(b, dn);                   // column L + 33 (none for lane 31)
+  if (lane == 0) r.wa = 0;
+  if (lane == 31) r.eb = 0;
+  return r;
+}
+
+// Neighbourhood of every sample of a column at the moment it is coded in a
+// pass: samples coded earlier in the pass (the column to the west, the row
+// above in the same column, and the row above the stripe) in their state
+// after it (f), the others in their state before it (p); the row below the
+// stripe is taken before the pass. fc/pc: this column; fw/pw: the column to
+// the west; fe/pe: to the east.
+struct Hood {
+  uint64_t nw, n, ne, w, e, sw, s, se;
+};
+__device__ __forceinline__ Hood hood(uint64_t fc, uint64_t pc, uint64_t fw, uint64_t pw, uint64_t fe, uint64_t pe) {
+  Hood h;
+  h.n = fc << 1;
+  h.s = pc >> 1;
+  h.w = fw;
+  h.e = pe;
+  h.nw = fw << 1;
+  h.ne = ((pe << 1) & ~kRow0) | ((fe << 1) & kRow0);
+  h.sw = ((fw >> 1) & ~kRow3) | ((pw >> 1) & kRow3);
+  h.se = pe >> 1;
+  return h;
+}
+
+__device__ __forceinline__ uint64_t pick(uint64_t m, uint64_t a, uint64_t b) { return (a & m) | (b & ~m); }
+
+// Symbol planes of one column: which pass codes each sample, its primary
+// symbol (context << 1 | magnitude bit) and its sign symbol, as bit-planes.
+enum Plane {
+  kPlV = 0,   // coded in significance propagation
+  kPlS,       // coded in magnitude refinement (significant before the plane)
+  kPlC,       // coded in cleanup
+  kPlB,       // magnitude bit of the plane
+  kPlClean,   // bit 4s: the column's part of stripe s is a cleanup run
+  kPlP0,      // primary context, bits 0..4
+  kPlP1,
+  kPlP2,
+  kPlP3,
+  kPlP4,
+  kPlM0,      // sign context - 8, bits 0..2
+  kPlM1,
+  kPlM2,
+  kPlX,       // sign ^ sign prediction
+  kNumPlanes
+};
+
+// Shared memory of one warp: the planes of its 64 columns, split in the
+// 32-bit halves of rows 0-31 and 32-63 (bank-conflict-free per half).
 struct ModelSmem {
-  uint64_t S[68];   // significant before this bit-plane; row y at y+1
-  uint64_t N[68];   // became significant in SP; row y at y+1
-  uint64_t Q[68];   // became significant in CL; row y at y+1
-  uint64_t Sn[68];  // coefficient sign; row y at y+1
-  uint64_t B[64];   // magnitude bit p
-  uint64_t R[64];   // refinement history (|q| >> (p+2) != 0)
-  uint64_t V[64];   // visited (coded) in SP
+  uint32_t pl[kNumPlanes][2][64];
 };
 
-// Each lane codes two adjacent columns, xa = 2 lane and xb = 2 lane + 1. A
-// row mask is seen through the lane's 4-bit window of columns
-// (xa-1, xa, xb, xb+1): bit 0 is the west neighbour of xa, bits 1-2 the
-// lane's own columns, bit 3 the east neighbour of xb (0 outside the block).
-__device__ __forceinline__ uint32_t win4(uint64_t m, int sh) {  // sh = 2 lane - 1
-  return (uint32_t)(sh < 0 ? (m << 1) : (m >> sh)) & 0xfu;
-}
+// Nibble (4 rows of stripe s) of a half-plane, s counted within the half.
+__device__ __forceinline__ uint32_t nib(uint32_t v, int s) { return (v >> (4 * s)) & 0xfu; }
+// The 4 bits of a nibble spread to bit 0 of each byte.
+__device__ __forceinline__ uint32_t spread4(uint32_t n) { return (n * 0x00204081u) & 0x01010101u; }
 
-// Zero-coding neighbourhood index (bit 0 NW, 1 N, 2 NE, 3 W, 5 E, 6 SW, 7 S,
-// 8 SE) of column c (0: xa, 1: xb) from windows of the row above, the row and
-// the row below. `f` windows hold the state of samples already visited in
-// this pass (west columns, and the rows above in the same column), `p`
-// windows the state before the pass (east columns, rows below).
-__device__ __forceinline__ uint32_t zc_index(uint32_t up_f, uint32_t up_p, uint32_t f, uint32_t pr,
-                                             uint32_t dn_f, uint32_t dn_p, int c) {
-  const uint32_t up = ((up_f >> c) & 3u) | ((up_p >> c) & 4u);
-  const uint32_t mid = (((f >> c) & 1u) << 3) | (((pr >> c) & 4u) << 3);
-  const uint32_t dn = (((dn_f >> c) & 1u) | ((dn_p >> c) & 6u)) << 6;
-  return up | mid | dn;
-}
-
-// Sign-context index from the four cardinal neighbours' significance and
-// sign at the moment the sign is coded (src/tier1/helpers.rs:52-88).
-__device__ __forceinline__ uint32_t sign_index(uint32_t sw, uint32_t gw, uint32_t sn, uint32_t gn,
-                                               uint32_t se, uint32_t ge, uint32_t ss, uint32_t gs) {
-  return (sw << 3) | ((sw & gw) << 0) | (sn << 1) | ((sn & gn) << 4) | (se << 5) | ((se & ge) << 2) |
-         (ss << 7) | ((ss & gs) << 6);
-}
-
-struct ModelTables {
-  const uint8_t* zc;  // orientation row
-  const uint8_t* sc;
-  const uint8_t* spb;
-};
-
-// Sign symbol of column c of a row: m8 is the sample's zero-coding index
-// (its N, W, E, S bits are the significance the sign context sees); g, gu,
-// gd are the sign windows of the row, the row above and the row below.
-__device__ __forceinline__ uint32_t sign_symbol(const ModelTables& t, uint32_t m8, uint32_t g,
-                                                uint32_t gu, uint32_t gd, int c) {
-  const uint32_t sw = (m8 >> 3) & 1u, sn = (m8 >> 1) & 1u, se = (m8 >> 5) & 1u, ss = (m8 >> 7) & 1u;
-  const uint32_t gw = (g >> c) & 1u, ge = (g >> (c + 2)) & 1u;
-  const uint32_t gn = (gu >> (c + 1)) & 1u, gs = (gd >> (c + 1)) & 1u;
-  const uint32_t lu = sign_index(sw, gw, sn, gn, se, ge, ss, gs);
-  return ((uint32_t)t.sc[lu] << 1) | (((g >> (c + 1)) & 1u) ^ t.spb[lu]);
-}
-
-// a[i] for a runtime i without indexing a register array (which would move
-// the array to local memory).
-__device__ __forceinline__ uint32_t pick4(const uint32_t (&a)[4], int i) {
-  return i < 2 ? (i == 0 ? a[0] : a[1]) : (i == 2 ? a[2] : a[3]);
-}
-__device__ __forceinline__ uint32_t pick6(const uint32_t (&a)[6], int i) {
-  return i < 3 ? (i == 0 ? a[0] : (i == 1 ? a[1] : a[2])) : (i == 3 ? a[3] : (i == 4 ? a[4] : a[5]));
+// Symbols of one column of one stripe: the column's counts per pass.
+__device__ __forceinline__ uint32_t column_counts(uint32_t v, uint32_t sm, uint32_t c, uint32_t b, uint32_t cl) {
+  const uint32_t sp = __popc(v) + __popc(v & b), mr = __popc(sm);
+  uint32_t cln;
+  if (cl) {
+    if (b == 0) {
+      cln = 1;
+    } else {
+      const uint32_t after = 0xfu & ~((2u << (__ffs(b) - 1)) - 1u);
+      cln = 4 + __popc(after) + __popc(after & b);
+    }
+  } else {
+    cln = __popc(c) + __popc(c & b);
+  }
+  return sp | (mr << 11) | (cln << 21);
 }
 
 // Exclusive prefix of v over the warp's lanes; *total = the warp's sum.
@@ -175,292 +208,260 @@ __device__ __forceinline__ uint32_t warp_offset(uint32_t v, int lane, uint32_t* 
   return x - v;
 }
 
-__global__ void __launch_bounds__(kModelWarps * 32, 3) t1_model_kernel(T1Args a) {
-  __shared__ ModelSmem sm_all[kModelWarps];
-  __shared__ uint8_t s_zc[4 * 512];
-  __shared__ uint8_t s_sc[256];
-  __shared__ uint8_t s_spb[256];
-  for (int i = threadIdx.x; i < 4 * 512; i += blockDim.x) s_zc[i] = c_tables.zc[i];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-    s_sc[i] = c_tables.sc[i];
-    s_spb[i] = c_tables.spb[i];
+// Writes the symbols of one column of one stripe into the three streams.
+__device__ __forceinline__ void emit_column(uint32_t v, uint32_t sm, uint32_t c, uint32_t b, uint32_t cl,
+                                            uint32_t prim, uint32_t sgn, uint8_t*& osp, uint8_t*& omr,
+                                            uint8_t*& ocl) {
+  int first = 0;  // rows consumed by a cleanup run
+  if (cl) {
+    if (b == 0) {
+      *ocl++ = (uint8_t)((uint32_t)kCtxAGG << 1);
+      first = 4;
+    } else {
+      const int rl = __ffs(b) - 1;
+      ocl[0] = (uint8_t)(((uint32_t)kCtxAGG << 1) | 1u);
+      ocl[1] = (uint8_t)(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl >> 1));
+      ocl[2] = (uint8_t)(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl & 1u));
+      ocl[3] = (uint8_t)(sgn >> (8 * rl));  // sign of the run's first significant sample
+      ocl += 4;
+      first = rl + 1;
+    }
   }
-  __syncthreads();
+  #pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint8_t p = (uint8_t)(prim >> (8 * r)), g = (uint8_t)(sgn >> (8 * r));
+    const bool bit = (b >> r) & 1u;
+    if ((sm >> r) & 1u) {
+      *omr++ = p;
+    } else if ((v >> r) & 1u) {
+      *osp++ = p;
+      if (bit) *osp++ = g;
+    } else if (r >= first && ((c >> r) & 1u)) {
+      *ocl++ = p;
+      if (bit) *ocl++ = g;
+    }
+  }
+}
 
+// One warp per (code-block, bit-plane) item.
+//
+// 1. Column masks of the plane: significant before it (|q| >> (p+1) != 0),
+//    magnitude bit p, refinement history (|q| >> (p+2) != 0), sign.
+// 2. Significance propagation: the visited (V) and newly significant (N)
+//    samples are the least fixpoint of the pass's visiting rule, iterated
+//    over the whole block; each round also fills every newly significant
+//    sample's run of magnitude-1 samples below it with one carry-propagating
+//    addition, so only horizontal chains take extra rounds. The scan order
+//    makes the rule causal, so the fixpoint is the sequential pass's result.
+// 3. Cleanup masks, run-length columns and, bit-sliced, every sample's
+//    symbols: zero-coding label with the neighbourhood of the pass that codes
+//    it, refinement context, sign context and prediction bit.
+// 4. Emission, stripe by stripe: each sample is coded in exactly one pass
+//    (SP if visited, MR if significant before, else cleanup or a cleanup
+//    run), so each lane writes its two columns' symbols into the three
+//    streams (SP | MR | cleanup, whose starts are known from the totals) at
+//    offsets from two packed warp scans.
+__global__ void __launch_bounds__(kModelWarps * 32, 6) t1_model_kernel(T1Args a) {
+  __shared__ ModelSmem sm_all[kModelWarps];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
-  ModelSmem& s = sm_all[wid];
+  ModelSmem& sm = sm_all[wid];
   const uint32_t nwarps = gridDim.x * kModelWarps;
+  const int xa = lane, xb = lane + 32;
 
   for (uint32_t item = blockIdx.x * kModelWarps + wid; item < a.nitems; item += nwarps) {
-    const uint32_t b = a.items[item];
-    const BlockDesc d = a.blocks[b];
+    const uint32_t blkno = a.items[item];
+    const BlockDesc d = a.blocks[blkno];
     const int w = d.w, h = d.h;
-    const int mbp = a.res[b].mbp;
-    const int j = (int)(item - a.plane_base[b]);
+    const int mbp = a.res[blkno].mbp;
+    const int j = (int)(item - a.plane_base[blkno]);
     const int p = mbp - 1 - j;
     const bool top = j == 0;
-    const uint64_t valid = w == 64 ? ~0ull : ((1ull << w) - 1);
     const int32_t* blk = a.coef + (size_t)d.coef_slot * a.cbw * a.cbh;
-    ModelTables t{s_zc + d.orient * 512, s_sc, s_spb};
-    const int sh = 2 * lane - 1;  // window of columns 2 lane - 1 .. 2 lane + 2
+    const uint64_t rows = h >= 64 ? ~0ull : ((1ull << h) - 1);
+    const uint64_t vA = xa < w ? rows : 0, vB = xb < w ? rows : 0;
 
-    // ---- masks for this bit-plane ----
-    for (int y = 0; y < h; ++y) {
-      int32_t v0 = lane < w ? blk[y * a.cbw + lane] : 0;
-      int32_t v1 = lane + 32 < w ? blk[y * a.cbw + lane + 32] : 0;
-      uint32_t m0 = v0 < 0 ? 0u - (uint32_t)v0 : (uint32_t)v0;
-      uint32_t m1 = v1 < 0 ? 0u - (uint32_t)v1 : (uint32_t)v1;
-      uint64_t sg = (uint64_t)__ballot_sync(~0u, (m0 >> (p + 1)) != 0) |
-                    ((uint64_t)__ballot_sync(~0u, (m1 >> (p + 1)) != 0) << 32);
-      uint64_t bt = (uint64_t)__ballot_sync(~0u, (m0 >> p) & 1) |
-                    ((uint64_t)__ballot_sync(~0u, (m1 >> p) & 1) << 32);
-      uint64_t rf = (uint64_t)__ballot_sync(~0u, p + 2 < 32 && (m0 >> (p + 2)) != 0) |
-                    ((uint64_t)__ballot_sync(~0u, p + 2 < 32 && (m1 >> (p + 2)) != 0) << 32);
-      uint64_t sn = (uint64_t)__ballot_sync(~0u, v0 < 0) | ((uint64_t)__ballot_sync(~0u, v1 < 0) << 32);
-      if (lane == 0) {
-        s.S[y + 1] = sg;
-        s.B[y] = bt;
-        s.R[y] = rf;
-        s.Sn[y + 1] = sn;
+    // ---- 1. column masks ----
+    uint64_t SA = 0, SB = 0, BA = 0, BB = 0, RA = 0, RB = 0, GA = 0, GB = 0;
+    {
+      const uint64_t tS = 1ull << (p + 1), tR = 1ull << (p + 2);
+      for (int y0 = 0; y0 < h; y0 += 8) {
+        int32_t qa[8], qb[8];
+        #pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int y = y0 + i;
+          qa[i] = y < h && xa < w ? blk[y * a.cbw + xa] : 0;
+          qb[i] = y < h && xb < w ? blk[y * a.cbw + xb] : 0;
+        }
+        #pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const uint64_t bit = 1ull << (y0 + i);
+          const uint32_t ma = qa[i] < 0 ? 0u - (uint32_t)qa[i] : (uint32_t)qa[i];
+          const uint32_t mb = qb[i] < 0 ? 0u - (uint32_t)qb[i] : (uint32_t)qb[i];
+          SA |= (uint64_t)ma >= tS ? bit : 0;
+          SB |= (uint64_t)mb >= tS ? bit : 0;
+          BA |= (ma >> p) & 1u ? bit : 0;
+          BB |= (mb >> p) & 1u ? bit : 0;
+          RA |= (uint64_t)ma >= tR ? bit : 0;
+          RB |= (uint64_t)mb >= tR ? bit : 0;
+          GA |= qa[i] < 0 ? bit : 0;
+          GB |= qb[i] < 0 ? bit : 0;
+        }
+      }
+    }
+    const Side sS = sides(SA, SB, lane);
+
+    // ---- 2. significance propagation ----
+    uint64_t NA = 0, NB = 0, VA = 0, VB = 0;
+    if (!top) {
+      // parts of the visiting rule on states before the pass: S below, E,
+      // SE, NE (rows 1-3 of a stripe), SW (row 3)
+      const uint64_t invA = (SA >> 1) | sS.ea | (sS.ea >> 1) | ((sS.ea << 1) & ~kRow0) | ((sS.wa >> 1) & kRow3);
+      const uint64_t invB = (SB >> 1) | sS.eb | (sS.eb >> 1) | ((sS.eb << 1) & ~kRow0) | ((sS.wb >> 1) & kRow3);
+      const uint64_t MA = BA & ~SA & vA, MB = BB & ~SB & vB;  // samples that turn significant when visited
+      for (;;) {  // N grows every round until it is stable: at most 4096 rounds
+        const uint64_t FA = SA | NA, FB = SB | NB;
+        const Side f = sides(FA, FB, lane);
+        VA = (invA | (FA << 1) | f.wa | (f.wa << 1) | ((f.wa >> 1) & ~kRow3) | ((f.ea << 1) & kRow0)) & ~SA & vA;
+        VB = (invB | (FB << 1) | f.wb | (f.wb << 1) | ((f.wb >> 1) & ~kRow3) | ((f.eb << 1) & kRow0)) & ~SB & vB;
+        uint64_t nA = VA & BA, nB = VB & BB;
+        nA |= MA & ~(MA + nA);  // the run of M below each new sample
+        nB |= MB & ~(MB + nB);
+        const bool changed = nA != NA || nB != NB;
+        NA = nA;
+        NB = nB;
+        if (!__any_sync(~0u, changed)) break;
+      }
+    }
+
+    // ---- 3. cleanup masks and the symbol planes ----
+    const uint64_t SNA = SA | NA, SNB = SB | NB;                // after SP
+    const uint64_t CA = ~SNA & ~VA & vA, CB = ~SNB & ~VB & vB;  // coded in cleanup
+    const uint64_t QA = CA & BA, QB = CB & BB;                  // significant in cleanup
+    const uint64_t FA = SNA | QA, FB = SNB | QB;                // after cleanup
+    const Side sSN = sides(SNA, SNB, lane), sF = sides(FA, FB, lane), sG = sides(GA, GB, lane);
+    uint32_t ns_sp = __popcll(NA) + __popcll(NB), ns_cl = __popcll(QA) + __popcll(QB);
+    uint32_t n_sp = __popcll(VA) + __popcll(VB) + ns_sp, sig_before = __popcll(SA) + __popcll(SB);
+    #pragma unroll
+    for (int col = 0; col < 2; ++col) {
+      const uint64_t S = col ? SB : SA, B = col ? BB : BA, R = col ? RB : RA, G = col ? GB : GA;
+      const uint64_t V = col ? VB : VA, SN = col ? SNB : SNA, C = col ? CB : CA, F = col ? FB : FA;
+      const uint64_t valid = col ? vB : vA;
+      const uint64_t Sw = col ? sS.wb : sS.wa, Se = col ? sS.eb : sS.ea;
+      const uint64_t SNw = col ? sSN.wb : sSN.wa, SNe = col ? sSN.eb : sSN.ea;
+      const uint64_t Fw = col ? sF.wb : sF.wa, Fe = col ? sF.eb : sF.ea;
+      const uint64_t Gw = col ? sG.wb : sG.wa, Ge = col ? sG.eb : sG.ea;
+      // cleanup runs (flags.rs:219-235): a full stripe of the column with
+      // nothing significant or visited in it or around it (west column and
+      // row above after cleanup, east column and row below before it)
+      const uint64_t T = SN | V | Fw | SNe | (((Fw | F | Fe) << 1) & kRow0) | (((SNw | SN | SNe) >> 1) & kRow3);
+      const uint64_t busy = (T | (T >> 1) | (T >> 2) | (T >> 3)) & kRow0;
+      const uint64_t clean = ~busy & kRow0 & (valid >> 3);
+      // neighbourhood at coding time: SP samples see the SP frames, the
+      // others the cleanup frames
+      const Hood hs = hood(SN, S, SNw, Sw, SNe, Se);
+      const Hood hc = hood(F, SN, Fw, SNw, Fe, SNe);
+      Hood hd;
+      hd.nw = pick(V, hs.nw, hc.nw);
+      hd.n = pick(V, hs.n, hc.n);
+      hd.ne = pick(V, hs.ne, hc.ne);
+      hd.w = pick(V, hs.w, hc.w);
+      hd.e = pick(V, hs.e, hc.e);
+      hd.sw = pick(V, hs.sw, hc.sw);
+      hd.s = pick(V, hs.s, hc.s);
+      hd.se = pick(V, hs.se, hc.se);
+      uint64_t l[4], m[3], x;
+      zc_label_planes(hd.nw, hd.n, hd.ne, hd.w, hd.e, hd.sw, hd.s, hd.se, (int)d.orient, l);
+      sign_planes(hd.n, hd.s, hd.w, hd.e, G << 1, G >> 1, Gw, Ge, m, &x);
+      // refinement context (helpers.rs:36-50): 16 after a first refinement,
+      // else 15 with a significant neighbour (state after SP), else 14
+      const uint64_t nb = (SN << 1) | (SN >> 1) | SNw | (SNw << 1) | (SNw >> 1) | SNe | (SNe << 1) | (SNe >> 1);
+      const uint64_t mr1 = S & ~R;  // contexts 14 and 15: binary 0111x
+      uint64_t out[kNumPlanes];
+      out[kPlV] = V;
+      out[kPlS] = S;
+      out[kPlC] = C;
+      out[kPlB] = B;
+      out[kPlClean] = clean;
+      out[kPlP0] = pick(S, mr1 & nb, l[0]);
+      out[kPlP1] = pick(S, mr1, l[1]);
+      out[kPlP2] = pick(S, mr1, l[2]);
+      out[kPlP3] = pick(S, mr1, l[3]);
+      out[kPlP4] = S & R;
+      out[kPlM0] = m[0];
+      out[kPlM1] = m[1];
+      out[kPlM2] = m[2];
+      out[kPlX] = x ^ G;
+      const int xc = col ? xb : xa;
+      #pragma unroll
+      for (int k = 0; k < kNumPlanes; ++k) {
+        sm.pl[k][0][xc] = (uint32_t)out[k];
+        sm.pl[k][1][xc] = (uint32_t)(out[k] >> 32);
+      }
+    }
+    n_sp = __reduce_add_sync(~0u, n_sp);
+    sig_before = __reduce_add_sync(~0u, sig_before);
+    ns_sp = __reduce_add_sync(~0u, ns_sp);
+    ns_cl = __reduce_add_sync(~0u, ns_cl);
+    __syncwarp();
+
+    // ---- 4. emission, stripe by stripe ----
+    uint8_t* out = a.sym + (size_t)item * a.sym_slot;
+    uint32_t pos_sp = 0, pos_mr = n_sp, pos_cl = n_sp + sig_before;
+    const int nstripes = (h + 3) >> 2;
+    for (int half = 0; half < 2 && 8 * half < nstripes; ++half) {
+      uint32_t qa[kNumPlanes], qb[kNumPlanes];
+      #pragma unroll
+      for (int k = 0; k < kNumPlanes; ++k) {
+        qa[k] = sm.pl[k][half][xa];
+        qb[k] = sm.pl[k][half][xb];
+      }
+      const int send = min(8, nstripes - 8 * half);
+      for (int s = 0; s < send; ++s) {
+        const uint32_t vA4 = nib(qa[kPlV], s), sA4 = nib(qa[kPlS], s), cA4 = nib(qa[kPlC], s),
+                       bA4 = nib(qa[kPlB], s), lA = nib(qa[kPlClean], s) & 1u;
+        const uint32_t vB4 = nib(qb[kPlV], s), sB4 = nib(qb[kPlS], s), cB4 = nib(qb[kPlC], s),
+                       bB4 = nib(qb[kPlB], s), lB = nib(qb[kPlClean], s) & 1u;
+        uint32_t totA, totB;
+        const uint32_t offA = warp_offset(column_counts(vA4, sA4, cA4, bA4, lA), lane, &totA);
+        const uint32_t offB = warp_offset(column_counts(vB4, sB4, cB4, bB4, lB), lane, &totB);
+        // primary and sign symbols of the 4 rows, one per byte
+        uint32_t primA = spread4(bA4), primB = spread4(bB4);
+        #pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          primA |= spread4(nib(qa[kPlP0 + k], s)) << (k + 1);
+          primB |= spread4(nib(qb[kPlP0 + k], s)) << (k + 1);
+        }
+        uint32_t sgnA = 0x10101010u | spread4(nib(qa[kPlX], s)), sgnB = 0x10101010u | spread4(nib(qb[kPlX], s));
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          sgnA |= spread4(nib(qa[kPlM0 + k], s)) << (k + 1);
+          sgnB |= spread4(nib(qb[kPlM0 + k], s)) << (k + 1);
+        }
+        uint8_t* osp = out + pos_sp + (offA & 0x7ffu);
+        uint8_t* omr = out + pos_mr + ((offA >> 11) & 0x3ffu);
+        uint8_t* ocl = out + pos_cl + (offA >> 21);
+        emit_column(vA4, sA4, cA4, bA4, lA, primA, sgnA, osp, omr, ocl);
+        osp = out + pos_sp + (totA & 0x7ffu) + (offB & 0x7ffu);
+        omr = out + pos_mr + ((totA >> 11) & 0x3ffu) + ((offB >> 11) & 0x3ffu);
+        ocl = out + pos_cl + (totA >> 21) + (offB >> 21);
+        emit_column(vB4, sB4, cB4, bB4, lB, primB, sgnB, osp, omr, ocl);
+        pos_sp += (totA & 0x7ffu) + (totB & 0x7ffu);
+        pos_mr += ((totA >> 11) & 0x3ffu) + ((totB >> 11) & 0x3ffu);
+        pos_cl += (totA >> 21) + (totB >> 21);
       }
     }
     if (lane == 0) {
-      s.S[0] = s.Sn[0] = s.N[0] = s.Q[0] = 0;
-    }
-    for (int y = h + 1 + lane; y < 68; y += 32) s.S[y] = s.Sn[y] = s.N[y] = s.Q[y] = 0;
-    __syncwarp();
-
-    uint8_t* out = a.sym + (size_t)item * a.sym_slot;
-    uint32_t pos = 0;
-    uint32_t n_sp = 0, n_mr = 0, ns_sp = 0, ns_cl = 0;
-    uint32_t sig_before = 0;
-    for (int y = lane; y < h; y += 32) sig_before += __popcll(s.S[y + 1]);
-    sig_before = __reduce_add_sync(~0u, sig_before);
-
-    if (!top) {
-      // ---- significance propagation: fixpoint per stripe ----
-      uint64_t Fp = 0;  // final SP state of the row above the stripe
-      for (int k = 0; k < h; k += 4) {
-        uint64_t S0 = s.S[k + 1], S1 = s.S[k + 2], S2 = s.S[k + 3], S3 = s.S[k + 4], D = s.S[k + 5];
-        uint64_t B0 = s.B[k], B1 = k + 1 < h ? s.B[k + 1] : 0, B2 = k + 2 < h ? s.B[k + 2] : 0,
-                 B3 = k + 3 < h ? s.B[k + 3] : 0;
-        uint64_t v0 = valid, v1 = k + 1 < h ? valid : 0, v2 = k + 2 < h ? valid : 0,
-                 v3 = k + 3 < h ? valid : 0;
-        if (k + 4 > h) D = 0;
-        uint64_t N0 = 0, N1 = 0, N2 = 0, N3 = 0, V0, V1, V2, V3;
-        for (;;) {
-          uint64_t F0 = S0 | N0, F1 = S1 | N1, F2 = S2 | N2, F3 = S3 | N3;
-          uint64_t vis0 = dil(Fp) | westm(F0) | eastm(S0) | westm(F1) | S1 | eastm(S1);
-          uint64_t vis1 = westm(F0) | F0 | eastm(S0) | westm(F1) | eastm(S1) | westm(F2) | S2 | eastm(S2);
-          uint64_t vis2 = westm(F1) | F1 | eastm(S1) | westm(F2) | eastm(S2) | westm(F3) | S3 | eastm(S3);
-          uint64_t vis3 = westm(F2) | F2 | eastm(S2) | westm(F3) | eastm(S3) | dil(D);
-          V0 = ~S0 & vis0 & v0; V1 = ~S1 & vis1 & v1; V2 = ~S2 & vis2 & v2; V3 = ~S3 & vis3 & v3;
-          uint64_t n0 = V0 & B0, n1 = V1 & B1, n2 = V2 & B2, n3 = V3 & B3;
-          if (n0 == N0 && n1 == N1 && n2 == N2 && n3 == N3) break;
-          N0 = n0; N1 = n1; N2 = n2; N3 = n3;
-        }
-        if (lane == 0) {
-          s.N[k + 1] = N0; s.N[k + 2] = N1; s.N[k + 3] = N2; s.N[k + 4] = N3;
-          s.V[k] = V0;
-          if (k + 1 < 64) s.V[k + 1] = V1;
-          if (k + 2 < 64) s.V[k + 2] = V2;
-          if (k + 3 < 64) s.V[k + 3] = V3;
-        }
-        ns_sp += __popcll(N0) + __popcll(N1) + __popcll(N2) + __popcll(N3);
-        // emission in scan order: within the stripe column by column (each
-        // lane: its column xa, then xb), rows top to bottom
-        const uint64_t F0 = S0 | N0, F1 = S1 | N1, F2 = S2 | N2, F3 = S3 | N3;
-        if (V0 | V1 | V2 | V3) {  // same masks in every lane: a uniform skip of empty stripes
-          const uint32_t wfp = win4(Fp, sh), wd = win4(D, sh);
-          const uint32_t wf[4] = {win4(F0, sh), win4(F1, sh), win4(F2, sh), win4(F3, sh)};
-          const uint32_t wp[4] = {win4(S0, sh), win4(S1, sh), win4(S2, sh), win4(S3, sh)};
-          const uint32_t wv[4] = {win4(V0, sh), win4(V1, sh), win4(V2, sh), win4(V3, sh)};
-          const uint32_t wb[4] = {win4(B0, sh), win4(B1, sh), win4(B2, sh), win4(B3, sh)};
-          uint32_t wg[6];
-          #pragma unroll
-          for (int r = 0; r < 6; ++r) wg[r] = win4(s.Sn[k + r], sh);  // rows k-1 .. k+4
-          uint32_t cnt = 0;
-          #pragma unroll
-          for (int r = 0; r < 4; ++r) cnt += __popc(wv[r] & 6u) + __popc(wv[r] & wb[r] & 6u);
-          uint32_t total;
-          uint8_t* o = out + pos + warp_offset(cnt, lane, &total);
-          pos += total;
-          n_sp += total;
-          #pragma unroll 1
-          for (int c = 0; c < 2; ++c) {
-            #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-              if (!((wv[r] >> (c + 1)) & 1u)) continue;
-              const uint32_t uf = r == 0 ? wfp : wf[r > 0 ? r - 1 : 0], up = r == 0 ? wfp : wp[r > 0 ? r - 1 : 0];
-              const uint32_t df = r == 3 ? wd : wf[r < 3 ? r + 1 : 3], dp = r == 3 ? wd : wp[r < 3 ? r + 1 : 3];
-              const uint32_t m8 = zc_index(uf, up, wf[r], wp[r], df, dp, c);
-              const uint32_t bit = (wb[r] >> (c + 1)) & 1u;
-              *o++ = (uint8_t)(((uint32_t)t.zc[m8] << 1) | bit);
-              if (bit) *o++ = (uint8_t)sign_symbol(t, m8, wg[r + 1], wg[r], wg[r + 2], c);
-            }
-          }
-        }
-        Fp = F3;
-        if (k + 4 > h) break;
-      }
-      __syncwarp();
-      // ---- magnitude refinement ----
-      for (int k = 0; k < h; k += 4) {
-        if (!(s.S[k + 1] | s.S[k + 2] | s.S[k + 3] | s.S[k + 4])) continue;  // nothing to refine
-        uint32_t wf[6];  // state after SP of rows k-1 .. k+4
-        #pragma unroll
-        for (int r = 0; r < 6; ++r) wf[r] = win4(s.S[k + r] | s.N[k + r], sh);
-        uint32_t ws[4], wr[4], wb[4];
-        #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          ws[r] = win4(s.S[k + r + 1], sh);
-          wr[r] = win4(s.R[k + r], sh);
-          wb[r] = win4(s.B[k + r], sh);
-        }
-        uint32_t cnt = 0;
-        #pragma unroll
-        for (int r = 0; r < 4; ++r) cnt += __popc(ws[r] & 6u);
-        uint32_t total;
-        uint8_t* o = out + pos + warp_offset(cnt, lane, &total);
-        pos += total;
-        n_mr += total;
-        #pragma unroll 1
-        for (int c = 0; c < 2; ++c) {
-          #pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            if (!((ws[r] >> (c + 1)) & 1u)) continue;
-            const uint32_t nb = ((wf[r] >> c) & 7u) | ((wf[r + 1] >> c) & 5u) | ((wf[r + 2] >> c) & 7u);
-            const uint32_t cx = ((wr[r] >> (c + 1)) & 1u) ? 16u : (nb ? 15u : 14u);  // helpers.rs:36-50
-            *o++ = (uint8_t)((cx << 1) | ((wb[r] >> (c + 1)) & 1u));
-          }
-        }
-      }
-    } else {
-      for (int y = lane; y < 64; y += 32) s.V[y] = 0;
-      for (int y = lane; y < 68; y += 32) s.N[y] = 0;
-      __syncwarp();
-    }
-
-    // ---- cleanup ----
-    {
-      uint64_t Gp = 0;  // final state (after this cleanup) of the row above
-      const uint32_t start = pos;
-      for (int k = 0; k < h; k += 4) {
-        const int lim = min(4, h - k);
-        uint64_t Gr[4], Vr[4], Br[4], Cr[4], Qr[4], Fr[4], Sg[4];
-        for (int r = 0; r < 4; ++r) {
-          const bool in = r < lim;
-          Gr[r] = in ? (s.S[k + r + 1] | s.N[k + r + 1]) : 0;
-          Vr[r] = in ? s.V[k + r] : 0;
-          Br[r] = in ? s.B[k + r] : 0;
-          Sg[r] = s.Sn[k + r + 1];
-          Cr[r] = in ? (~Gr[r] & ~Vr[r] & valid) : 0;
-          Qr[r] = Cr[r] & Br[r];
-          Fr[r] = Gr[r] | Qr[r];
-        }
-        const uint64_t Gd = lim == 4 && k + 4 < h ? (s.S[k + 5] | s.N[k + 5]) : 0;  // next stripe, pre-CL
-        const uint64_t SgP = s.Sn[k], SgD = s.Sn[k + 5];
-        ns_cl += __popcll(Qr[0]) + __popcll(Qr[1]) + __popcll(Qr[2]) + __popcll(Qr[3]);
-        if (lane == 0) {
-          #pragma unroll
-          for (int r = 0; r < 4; ++r)
-            if (r < lim) s.Q[k + r + 1] = Qr[r];
-        }
-        // run-length eligibility of each column (flags.rs:219-235)
-        uint64_t clean = 0;
-        if (lim == 4) {
-          uint64_t busy = Gr[0] | Gr[1] | Gr[2] | Gr[3] | Vr[0] | Vr[1] | Vr[2] | Vr[3];
-          uint64_t nbr = dil(Gp) | westm(Fr[0] | Fr[1] | Fr[2] | Fr[3]) |
-                         eastm(Gr[0] | Gr[1] | Gr[2] | Gr[3]) | dil(Gd);
-          clean = ~(busy | nbr) & valid;
-        }
-        if (Cr[0] | Cr[1] | Cr[2] | Cr[3]) {  // any sample left to code in this stripe
-          const uint32_t wgp = win4(Gp, sh), wgd = win4(Gd, sh), wcl = win4(clean, sh);
-          uint32_t wG[4], wF[4], wC[4], wB[4], wsg[6];
-          #pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            wG[r] = win4(Gr[r], sh);
-            wF[r] = win4(Fr[r], sh);
-            wC[r] = win4(Cr[r], sh);
-            wB[r] = win4(Br[r], sh);
-          }
-          wsg[0] = win4(SgP, sh);
-          #pragma unroll
-          for (int r = 0; r < 4; ++r) wsg[r + 1] = win4(Sg[r], sh);
-          wsg[5] = win4(SgD, sh);
-          // per column: candidate rows (4-bit), their bits, run-mode eligibility
-          auto col_bits = [&](const uint32_t (&wv)[4], int c) {
-            uint32_t m = 0;
-            #pragma unroll
-            for (int r = 0; r < 4; ++r) m |= ((wv[r] >> (c + 1)) & 1u) << r;
-            return m;
-          };
-          uint32_t cnt = 0;
-          #pragma unroll
-          for (int c = 0; c < 2; ++c) {
-            const uint32_t cmc = col_bits(wC, c), bmc = col_bits(wB, c);
-            if ((wcl >> (c + 1)) & 1u) {
-              if (bmc == 0) {
-                cnt += 1;
-              } else {
-                const uint32_t after = 0xfu & ~((2u << (__ffs(bmc) - 1)) - 1u);
-                cnt += 4 + __popc(after) + __popc(bmc & after);
-              }
-            } else {
-              cnt += __popc(cmc) + __popc(cmc & bmc);
-            }
-          }
-          uint32_t total;
-          uint8_t* o = out + pos + warp_offset(cnt, lane, &total);
-          pos += total;
-          #pragma unroll 1
-          for (int c = 0; c < 2; ++c) {
-            const uint32_t cmc = col_bits(wC, c), bmc = col_bits(wB, c);
-            int first = 0;
-            if ((wcl >> (c + 1)) & 1u) {
-              if (bmc == 0) {
-                *o++ = (uint8_t)((uint32_t)kCtxAGG << 1);
-                first = 4;
-              } else {
-                const int rl = __ffs(bmc) - 1;
-                *o++ = (uint8_t)(((uint32_t)kCtxAGG << 1) | 1u);
-                *o++ = (uint8_t)(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl >> 1));
-                *o++ = (uint8_t)(((uint32_t)kCtxUNI << 1) | ((uint32_t)rl & 1u));
-                // sign of the run's first significant sample
-                const uint32_t uf = rl == 0 ? wgp : pick4(wF, rl - 1), up = rl == 0 ? wgp : pick4(wG, rl - 1);
-                const uint32_t df = rl == 3 ? wgd : pick4(wF, rl + 1), dp = rl == 3 ? wgd : pick4(wG, rl + 1);
-                const uint32_t m8 = zc_index(uf, up, pick4(wF, rl), pick4(wG, rl), df, dp, c);
-                *o++ = (uint8_t)sign_symbol(t, m8, pick6(wsg, rl + 1), pick6(wsg, rl), pick6(wsg, rl + 2), c);
-                first = rl + 1;
-              }
-            }
-            #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-              if (r < first || !((cmc >> r) & 1u)) continue;
-              const uint32_t uf = r == 0 ? wgp : wF[r > 0 ? r - 1 : 0], up = r == 0 ? wgp : wG[r > 0 ? r - 1 : 0];
-              const uint32_t df = r == 3 ? wgd : wF[r < 3 ? r + 1 : 3], dp = r == 3 ? wgd : wG[r < 3 ? r + 1 : 3];
-              const uint32_t m8 = zc_index(uf, up, wF[r], wG[r], df, dp, c);
-              const uint32_t bit = (bmc >> r) & 1u;
-              *o++ = (uint8_t)(((uint32_t)t.zc[m8] << 1) | bit);
-              if (bit) *o++ = (uint8_t)sign_symbol(t, m8, wsg[r + 1], wsg[r], wsg[r + 2], c);
-            }
-          }
-        }
-        Gp = lim == 4 ? Fr[3] : (lim == 3 ? Fr[2] : (lim == 2 ? Fr[1] : Fr[0]));
-      }
-      if (lane == 0) {
-        ItemRec rec;
-        rec.n_sp = n_sp;
-        rec.n_mr = n_mr;
-        rec.n_cl = pos - start;
-        rec.ns_sp = ns_sp;
-        rec.ns_cl = ns_cl;
-        rec.sig_before = sig_before;
-        rec.bitplane = (uint32_t)p;
-        rec.pad = 0;
-        a.item_rec[item] = rec;
-      }
+      ItemRec rec;
+      rec.n_sp = n_sp;
+      rec.n_mr = sig_before;
+      rec.n_cl = pos_cl - (n_sp + sig_before);
+      rec.ns_sp = ns_sp;
+      rec.ns_cl = ns_cl;
+      rec.sig_before = sig_before;
+      rec.bitplane = (uint32_t)p;
+      rec.pad = 0;
+      a.item_rec[item] = rec;
     }
     __syncwarp();
   }
@@ -1058,6 +1059,26 @@ __global__ void __launch_bounds__(kMqWarps * 32) t1_mq_pull_kernel(T1Args a, uin
 
 }  // namespace
 
+// The bit-sliced context formation evaluated on single samples, in the
+// layout of the context tables (jp2g_debug_context_labels).
+void context_labels_from_logic(uint8_t* zc, uint8_t* sc, uint8_t* spb) {
+  for (int o = 0; o < 4; ++o)
+    for (uint32_t f = 0; f < 512; ++f) {
+      uint32_t l[4];
+      zc_label_planes<uint32_t>(f & 1u, (f >> 1) & 1u, (f >> 2) & 1u, (f >> 3) & 1u, (f >> 5) & 1u,
+                                (f >> 6) & 1u, (f >> 7) & 1u, (f >> 8) & 1u, o, l);
+      zc[o * 512 + f] = (uint8_t)((l[0] & 1u) | (l[1] & 1u) << 1 | (l[2] & 1u) << 2 | (l[3] & 1u) << 3);
+    }
+  // sign index: bit 3 W, 0 W negative, 1 N, 4 N negative, 5 E, 2 E negative, 7 S, 6 S negative
+  for (uint32_t f = 0; f < 256; ++f) {
+    uint32_t m[3], x;
+    sign_planes<uint32_t>((f >> 1) & 1u, (f >> 7) & 1u, (f >> 3) & 1u, (f >> 5) & 1u, (f >> 4) & 1u, (f >> 6) & 1u,
+                          f & 1u, (f >> 2) & 1u, m, &x);
+    sc[f] = (uint8_t)(8u + ((m[0] & 1u) | (m[1] & 1u) << 1 | (m[2] & 1u) << 2));
+    spb[f] = (uint8_t)(x & 1u);
+  }
+}
+
 bool upload_t1_tables(const uint8_t* zc, const uint8_t* sc, const uint8_t* spb,
                       const uint32_t* mq) {
   Tables t;
@@ -1083,7 +1104,7 @@ void launch_t1_items(const T1Args& a, cudaStream_t st) {
 void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st) {
   if (a.nitems == 0) return;
   uint32_t need = (a.nitems + kModelWarps - 1) / kModelWarps;
-  uint32_t cap = (uint32_t)num_sms * 8;
+  uint32_t cap = (uint32_t)num_sms * 6 * 4;  // CTAs loop over the items
   t1_model_kernel<<<need < cap ? need : cap, kModelWarps * 32, 0, st>>>(a);
 }
 

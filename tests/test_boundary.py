@@ -104,3 +104,16 @@ def test_synthetic_page_is_deterministic():
     assert bg.size > 0.6 * a.size
     c = _native.synth_page(256, 192, 3, 5, photo_w=120, photo_h=90)
     assert c.size == 256 * 192 * 3
+
+
+def test_bit_sliced_context_logic_equals_the_context_tables():
+    # the modelling kernel forms zero-coding labels, sign contexts and sign
+    # predictions with bit-sliced logic; on every neighbourhood it must give
+    # the tables' entries (which equal the reference's literal tables)
+    zc, sc, spb, _ = _native.tables()
+    lz, ls, lp = _native.context_labels()
+    for o in range(4):
+        for f in range(512):
+            assert lz[o * 512 + f] == zc[o * 512 + f], (o, f)
+    assert np.array_equal(ls, sc)
+    assert np.array_equal(lp, spb)
