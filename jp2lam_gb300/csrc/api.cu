@@ -97,8 +97,8 @@ struct jp2g_ctx {
   std::mutex mu;    // device pools and stream: one wave (or encode) at a time
   // device pools
   DevBuf px, ll0, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
-      hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, sym, stats, dwtargs,
-      dwtbases, mqorder, mqscratch;
+      hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, planes, signs, sym, stats,
+      dwtargs, dwtbases, mqorder, mqscratch;
   // pinned host staging
   HostBuf hpx, hpx2, hkeep, hoffsets, hbody, hres, hcount;
   bool timing = false;
@@ -668,12 +668,16 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
   ta.nitems = *reinterpret_cast<uint32_t*>(c->hcount.p);
   if (!reserve(c, c->items, std::max<size_t>(ta.nitems, 1) * 4) ||
       !reserve(c, c->itemrec, std::max<size_t>(ta.nitems, 1) * sizeof(ItemRec)) ||
+      !reserve(c, c->planes, std::max<size_t>(ta.nitems, 1) * 1024) ||
+      !reserve(c, c->signs, std::max<size_t>(nb, 1) * 512) ||
       !reserve(c, c->sym, std::max<size_t>(ta.nitems, 1) * ta.sym_slot + 64))  // the MQ reader runs 48 B ahead
     return kEncodeFailed;
   ta.items = dptr<uint32_t>(c->items);
   ta.item_rec = dptr<ItemRec>(c->itemrec);
+  ta.planes = dptr<uint32_t>(c->planes);
+  ta.signs = dptr<uint32_t>(c->signs);
   ta.sym = dptr<uint8_t>(c->sym);
-  launch_t1_items(ta, c->stream);
+  launch_t1_planes(ta, c->stream);
   record(c, kEvAnalyzeEnd);
   launch_t1_model(ta, c->num_sms, c->stream);
   record(c, kEvModelEnd);
@@ -807,8 +811,8 @@ void release_pools(jp2g_ctx* c) {
   DevBuf* bufs[] = {&c->px, &c->ll0, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
-                    &c->itemrec, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases, &c->mqorder,
-                    &c->mqscratch};
+                    &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
+                    &c->mqorder, &c->mqscratch};
   for (DevBuf* b : bufs) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -1015,8 +1019,8 @@ void jp2g_destroy(jp2g_ctx* c) {
   DevBuf* bufs[] = {&c->px, &c->ll0, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
-                    &c->itemrec, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases, &c->mqorder,
-                    &c->mqscratch};
+                    &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
+                    &c->mqorder, &c->mqscratch};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   HostBuf* hb[] = {&c->hpx, &c->hpx2, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres, &c->hcount};

@@ -59,6 +59,8 @@ struct T1Args {
   uint32_t* plane_base;  // per block: first item (exclusive prefix of nplanes)
   uint32_t* items;       // per item: its block
   uint32_t nitems;
+  uint32_t* planes;      // per item: column masks of its plane (t1_planes_kernel), 1 KiB
+  uint32_t* signs;       // per block: sign column masks, 512 B
   ItemRec* item_rec;
   uint8_t* sym;          // per item: a slot of sym_slot symbol bytes
   uint32_t sym_slot;
@@ -67,7 +69,8 @@ struct T1Args {
 };
 
 void launch_t1_analyze(const T1Args& a, cudaStream_t st);
-void launch_t1_items(const T1Args& a, cudaStream_t st);
+// Items list and per-item bit-plane column masks (after the plane-count scan).
+void launch_t1_planes(const T1Args& a, cudaStream_t st);
 void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st);
 // bpw: code-blocks per warp, 1..32, or 0 for automatic.
 void launch_t1_mq(const T1Args& a, int num_sms, int bpw, cudaStream_t st);

@@ -86,14 +86,69 @@ __global__ void t1_analyze_kernel(T1Args a) {
   a.nplanes[warp] = o.status ? 0u : (uint32_t)mbp;
 }
 
-__global__ void t1_items_kernel(T1Args a) {
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= a.nblocks) return;
-  const uint32_t base = a.plane_base[b], n = a.nplanes[b];
-  for (uint32_t j = 0; j < n; ++j) a.items[base + j] = b;
+// 32x32 bit-matrix transpose in registers: on entry bit j of t[i] is
+// element (i, j); on exit bit i of t[j] is.
+__device__ __forceinline__ void transpose32(uint32_t (&t)[32]) {
+  #pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const uint32_t m = s == 16 ? 0x0000ffffu : (s == 8 ? 0x00ff00ffu : (s == 4 ? 0x0f0f0f0fu : (s == 2 ? 0x33333333u : 0x55555555u)));
+    #pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      if (i & s) continue;
+      const uint32_t x = ((t[i] >> s) ^ t[i + s]) & m;
+      t[i] ^= x << s;
+      t[i + s] ^= x;
+    }
+  }
 }
 
-// ------------------------------------------------------------------ model --
+// One warp per code-block: lists the block's items and writes, for every
+// bit-plane p it codes, the column masks the modelling kernel starts from:
+// significant before the plane (|q| >> (p+1) != 0) and the magnitude bit p,
+// plus the block's sign masks. A lane reads 32 rows of one column, and a
+// transpose in registers turns 32 magnitudes into 32 bit-plane masks, so
+// every coefficient is read once per block instead of once per plane.
+// Layout: planes[((item * 2 + {0: S, 1: B}) * 2 + half) * 64 + column],
+// signs[(block * 2 + half) * 64 + column], half 0 = rows 0-31.
+__global__ void __launch_bounds__(256) t1_planes_kernel(T1Args a) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (b >= a.nblocks) return;
+  const uint32_t np = a.nplanes[b], base = a.plane_base[b];
+  for (uint32_t j = lane; j < np; j += 32) a.items[base + j] = b;
+  const BlockDesc d = a.blocks[b];
+  const int w = d.w, h = d.h, mbp = (int)np;
+  const int32_t* blk = a.coef + (size_t)d.coef_slot * a.cbw * a.cbh;
+  #pragma unroll 1
+  for (int col = 0; col < 2; ++col) {
+    const int x = lane + 32 * col;
+    #pragma unroll 1
+    for (int half = 0; half < 2; ++half) {
+      uint32_t t[32], sg = 0;
+      #pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const int y = 32 * half + i;
+        const int32_t q = y < h && x < w ? blk[y * a.cbw + x] : 0;
+        t[i] = q < 0 ? 0u - (uint32_t)q : (uint32_t)q;
+        sg |= q < 0 ? 1u << i : 0u;
+      }
+      a.signs[((size_t)b * 2 + half) * 64 + x] = sg;
+      if (mbp == 0) continue;
+      transpose32(t);
+      uint32_t above = 0;  // rows with a bit above plane k
+      #pragma unroll
+      for (int k = 31; k >= 0; --k) {
+        if (k < mbp) {
+          const size_t item = base + (uint32_t)(mbp - 1 - k);
+          a.planes[((item * 2 + 0) * 2 + half) * 64 + x] = above;
+          a.planes[((item * 2 + 1) * 2 + half) * 64 + x] = t[k];
+        }
+        above |= t[k];
+      }
+    }
+  }
+}
+
 // Modelling works on the code-block in column layout: lane L owns columns
 // L ("A") and L + 32 ("B"), and every per-sample state of a column is a
 // 64-bit mask with bit y = row y. Vertical neighbours are then shifts of the
@@ -227,19 +282,20 @@ __device__ __forceinline__ void emit_column(uint32_t v, uint32_t sm, uint32_t c,
       first = rl + 1;
     }
   }
+  // every row in the same predicated code: the lanes of a warp code
+  // samples of different passes at the same row
   #pragma unroll
   for (int r = 0; r < 4; ++r) {
-    const uint8_t p = (uint8_t)(prim >> (8 * r)), g = (uint8_t)(sgn >> (8 * r));
-    const bool bit = (b >> r) & 1u;
-    if ((sm >> r) & 1u) {
-      *omr++ = p;
-    } else if ((v >> r) & 1u) {
-      *osp++ = p;
-      if (bit) *osp++ = g;
-    } else if (r >= first && ((c >> r) & 1u)) {
-      *ocl++ = p;
-      if (bit) *ocl++ = g;
-    }
+    const uint32_t bit = (b >> r) & 1u;
+    const bool im = (sm >> r) & 1u;
+    const bool iv = (v >> r) & 1u;
+    const bool ic = r >= first && ((c >> r) & 1u);
+    uint8_t* o = im ? omr : (iv ? osp : ocl);
+    if (im | iv | ic) o[0] = (uint8_t)(prim >> (8 * r));
+    if ((iv | ic) && bit) o[1] = (uint8_t)(sgn >> (8 * r));
+    omr += im ? 1 : 0;
+    osp += iv ? 1 + bit : 0;
+    ocl += ic ? 1 + bit : 0;
   }
 }
 
@@ -277,38 +333,18 @@ __global__ void __launch_bounds__(kModelWarps * 32, 6) t1_model_kernel(T1Args a)
     const int j = (int)(item - a.plane_base[blkno]);
     const int p = mbp - 1 - j;
     const bool top = j == 0;
-    const int32_t* blk = a.coef + (size_t)d.coef_slot * a.cbw * a.cbh;
     const uint64_t rows = h >= 64 ? ~0ull : ((1ull << h) - 1);
     const uint64_t vA = xa < w ? rows : 0, vB = xb < w ? rows : 0;
 
-    // ---- 1. column masks ----
-    uint64_t SA = 0, SB = 0, BA = 0, BB = 0, RA = 0, RB = 0, GA = 0, GB = 0;
-    {
-      const uint64_t tS = 1ull << (p + 1), tR = 1ull << (p + 2);
-      for (int y0 = 0; y0 < h; y0 += 8) {
-        int32_t qa[8], qb[8];
-        #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int y = y0 + i;
-          qa[i] = y < h && xa < w ? blk[y * a.cbw + xa] : 0;
-          qb[i] = y < h && xb < w ? blk[y * a.cbw + xb] : 0;
-        }
-        #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const uint64_t bit = 1ull << (y0 + i);
-          const uint32_t ma = qa[i] < 0 ? 0u - (uint32_t)qa[i] : (uint32_t)qa[i];
-          const uint32_t mb = qb[i] < 0 ? 0u - (uint32_t)qb[i] : (uint32_t)qb[i];
-          SA |= (uint64_t)ma >= tS ? bit : 0;
-          SB |= (uint64_t)mb >= tS ? bit : 0;
-          BA |= (ma >> p) & 1u ? bit : 0;
-          BB |= (mb >> p) & 1u ? bit : 0;
-          RA |= (uint64_t)ma >= tR ? bit : 0;
-          RB |= (uint64_t)mb >= tR ? bit : 0;
-          GA |= qa[i] < 0 ? bit : 0;
-          GB |= qb[i] < 0 ? bit : 0;
-        }
-      }
-    }
+    // ---- 1. column masks (made by t1_planes_kernel) ----
+    auto ld = [&](const uint32_t* v, size_t row0, int x) {
+      return (uint64_t)v[row0 + x] | (uint64_t)v[row0 + 64 + x] << 32;
+    };
+    const size_t pi = (size_t)item * 256;
+    const uint64_t SA = ld(a.planes, pi, xa), SB = ld(a.planes, pi, xb);
+    const uint64_t BA = ld(a.planes, pi + 128, xa), BB = ld(a.planes, pi + 128, xb);
+    const uint64_t RA = top ? 0 : ld(a.planes, pi - 256, xa), RB = top ? 0 : ld(a.planes, pi - 256, xb);
+    const uint64_t GA = ld(a.signs, (size_t)blkno * 128, xa), GB = ld(a.signs, (size_t)blkno * 128, xb);
     const Side sS = sides(SA, SB, lane);
 
     // ---- 2. significance propagation ----
@@ -1096,9 +1132,9 @@ void launch_t1_analyze(const T1Args& a, cudaStream_t st) {
   t1_analyze_kernel<<<grid, threads, 0, st>>>(a);
 }
 
-void launch_t1_items(const T1Args& a, cudaStream_t st) {
+void launch_t1_planes(const T1Args& a, cudaStream_t st) {
   if (a.nblocks == 0) return;
-  t1_items_kernel<<<(a.nblocks + 255) / 256, 256, 0, st>>>(a);
+  t1_planes_kernel<<<(uint32_t)(((uint64_t)a.nblocks * 32 + 255) / 256), 256, 0, st>>>(a);
 }
 
 void launch_t1_model(const T1Args& a, int num_sms, cudaStream_t st) {
