@@ -60,6 +60,18 @@ void jp2g_destroy(jp2g_ctx* ctx);
 int jp2g_encode(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h, uint32_t ncomp,
                 int interleaved, uint8_t quality, int format, uint8_t** out, size_t* out_len);
 
+/* jp2g_encode plus the encode's quality metrics, as encode_with_psnr
+ * (src/encode/mod.rs:129-135) computes them (compute_quality_metrics,
+ * src/encode/backend/native/backend.rs:305-433): the retained bit-planes of
+ * every code-block dequantised at the midpoint, the inverse 9/7, inverse ICT
+ * and level shift give the decoded samples, all on the device; *psnr_db is
+ * their PSNR against the input (100 when the error is below 1e-10) and *ssim
+ * the mean SSIM of 8x8 luma blocks (1.0 when the page has none). Lossless
+ * encodes (quality >= 100) give +infinity and 1.0. */
+int jp2g_encode_with_psnr(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h, uint32_t ncomp,
+                          int interleaved, uint8_t quality, int format, uint8_t** out, size_t* out_len,
+                          double* psnr_db, double* ssim);
+
 /* Same as jp2g_encode, but `d_px` is interleaved pixel data already resident
  * in device memory (w * h * ncomp bytes). Used for device-resident batching;
  * the reference has no equivalent entry point (its input is always host
@@ -211,6 +223,11 @@ int jp2g_counters(jp2g_ctx* ctx, uint64_t* out, int n);
  * `comp` after colour transform, DWT and quantisation. */
 int jp2g_debug_coefficients(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,
                             uint32_t ncomp, uint8_t quality, uint32_t comp, int32_t* plane);
+/* The same plane before quantisation (lossy qualities only): the f32
+ * coefficients of the colour transform and 9/7 DWT, for comparing the
+ * pipeline against exact (FP64) lifting. */
+int jp2g_debug_coefficients_f32(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,
+                                uint32_t ncomp, uint8_t quality, uint32_t comp, float* plane);
 /* Per-block Tier-1 results in codestream order, 8 int32 per block:
  * (mbp, zbp, npasses, payload_len, cls, status, kept_passes, kept_bytes). */
 int jp2g_debug_blocks(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,

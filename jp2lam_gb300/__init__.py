@@ -7,6 +7,7 @@ backed by the C ABI in include/jp2g.h (libjp2g.so, CUDA for sm_103a):
     EncodeOptions(quality, format), Preset          (src/model.rs:41-177)
     encode(image, options) -> bytes                 (src/encode/mod.rs:84-101)
     encode_to_writer(image, options, writer)        (src/encode/mod.rs:103-113)
+    encode_with_psnr(image, options)                (src/encode/mod.rs:115-135)
     BatchEncoder(options).encode_one / encode_all   (src/batch.rs:26-85)
     encode_batch(images, options)                   (src/batch.rs:173-178)
 
@@ -25,7 +26,7 @@ from ._native import Engine, Jp2LamError, InvalidInput, EncodeFailed, DecodeFail
 
 __all__ = [
     "ColorSpace", "OutputFormat", "Preset", "Image", "Component", "EncodeOptions",
-    "encode", "encode_to_writer", "BatchEncoder", "BatchProfile", "encode_batch",
+    "encode", "encode_to_writer", "encode_with_psnr", "EncodeMetrics", "BatchEncoder", "BatchProfile", "encode_batch",
     "encode_pages", "Server", "Engine", "Jp2LamError", "InvalidInput", "EncodeFailed", "DecodeFailed",
     "UnsupportedFeature", "IoError",
 ]
@@ -146,6 +147,26 @@ def encode_to_writer(image: Image, options: EncodeOptions, writer) -> None:
         writer.write(data)
     except Exception as err:  # mirrors EncodeFailed(err.to_string())
         raise EncodeFailed(str(err)) from err
+
+
+@dataclass(frozen=True)
+class EncodeMetrics:
+    """src/encode/mod.rs:115-123: PSNR in dB (+inf for lossless) and the
+    mean SSIM of 8x8 luma blocks (1.0 for lossless)."""
+    psnr_db: float
+    ssim: float
+
+
+def encode_with_psnr(image: Image, options: EncodeOptions,
+                     engine: Optional[Engine] = None):
+    """Encode and compute the quality metrics in one call
+    (src/encode/mod.rs:129-135); the decoder-side reconstruction behind the
+    metrics runs on the GPU. Returns (bytes, EncodeMetrics)."""
+    _validate(image)
+    eng = engine or default_engine()
+    data, psnr, ssim = eng.encode_with_psnr(image.data, image.width, image.height, image.ncomp,
+                                            int(options.quality), int(options.format))
+    return data, EncodeMetrics(psnr, ssim)
 
 
 @dataclass(frozen=True)

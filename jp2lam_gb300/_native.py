@@ -52,6 +52,7 @@ EXPORTS = [
     "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
     "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
     "jp2g_autotune", "jp2g_debug_assemble", "jp2g_debug_plan", "jp2g_cancel", "jp2g_debug_context_labels",
+    "jp2g_debug_coefficients_f32", "jp2g_encode_with_psnr",
 ]
 
 PENDING = 6
@@ -104,6 +105,11 @@ def load_library(path: str = LIB_PATH):
         lib.jp2g_debug_coefficients.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                                 ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8,
                                                 ctypes.c_uint32, ctypes.c_void_p]
+        lib.jp2g_debug_coefficients_f32.argtypes = lib.jp2g_debug_coefficients.argtypes
+        lib.jp2g_encode_with_psnr.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
+                                              ctypes.c_uint32, ctypes.c_int, ctypes.c_uint8, ctypes.c_int,
+                                              ctypes.POINTER(_u8p), ctypes.POINTER(ctypes.c_size_t),
+                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         lib.jp2g_debug_blocks.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8,
                                           ctypes.c_void_p, ctypes.c_uint32,
@@ -182,6 +188,26 @@ class Engine:
         data = ctypes.string_at(out, n.value)
         self.lib.jp2g_free(out)
         return data
+
+    def encode_with_psnr(self, px, w: int, h: int, ncomp: int, quality: int, fmt: int,
+                         interleaved: bool = True):
+        """(codestream, psnr_db, ssim): the encode and its quality metrics,
+        computed on the device (encode_with_psnr, src/encode/mod.rs:129)."""
+        buf = np.frombuffer(px, dtype=np.uint8) if isinstance(px, (bytes, bytearray)) else \
+            np.ascontiguousarray(px, dtype=np.uint8)
+        if buf.size != w * h * ncomp:
+            raise InvalidInput("pixel buffer length does not match the image dimensions")
+        out = _u8p()
+        n = ctypes.c_size_t()
+        psnr, ssim = ctypes.c_double(), ctypes.c_double()
+        with self._lock:
+            rc = self.lib.jp2g_encode_with_psnr(self.handle, buf.ctypes.data_as(ctypes.c_void_p), w, h, ncomp,
+                                                int(interleaved), quality, fmt, ctypes.byref(out), ctypes.byref(n),
+                                                ctypes.byref(psnr), ctypes.byref(ssim))
+            self._check(rc)
+        data = ctypes.string_at(out, n.value)
+        self.lib.jp2g_free(out)
+        return data, psnr.value, ssim.value
 
     def encode_device(self, dev_ptr: int, w: int, h: int, ncomp: int, quality: int, fmt: int) -> bytes:
         out = _u8p()
@@ -324,6 +350,14 @@ class Engine:
                                                      ncomp, quality, comp,
                                                      plane.ctypes.data_as(ctypes.c_void_p)))
         return plane.reshape(h, w)
+
+    def debug_coefficients_f32(self, px, w, h, ncomp, quality, comp):
+        """Unquantised f32 coefficients (lossy qualities) of one component."""
+        px = np.ascontiguousarray(px, dtype=np.uint8)
+        out = np.zeros(w * h, np.float32)
+        self._check(self.lib.jp2g_debug_coefficients_f32(self.handle, px.ctypes.data_as(ctypes.c_void_p), w, h,
+                                                         ncomp, quality, comp, out.ctypes.data_as(ctypes.c_void_p)))
+        return out.reshape(h, w)
 
     def debug_blocks(self, px, w, h, ncomp, quality):
         px = np.ascontiguousarray(px, dtype=np.uint8)

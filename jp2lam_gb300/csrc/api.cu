@@ -10,6 +10,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
+#include <limits>
 #include <chrono>
 #include <condition_variable>
 #include <cstdlib>
@@ -98,7 +100,7 @@ struct jp2g_ctx {
   // device pools
   DevBuf px, ll0, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
       hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, planes, signs, sym, stats,
-      dwtargs, dwtbases, mqorder, mqscratch;
+      dwtargs, dwtbases, mqorder, mqscratch, recon, reconblk;
   // pinned host staging
   HostBuf hpx, hpx2, hkeep, hoffsets, hbody, hres, hcount;
   bool timing = false;
@@ -303,7 +305,7 @@ DwtLevelArgs level_args(const PagePlan& p, int l, const uint8_t* d_px, uint32_t 
 // launch over the tiles of all pages that have it (one per transform kind);
 // a page whose region at some level is under 2 samples wide or high, or that
 // has no decomposition level, takes the per-page kernel there.
-int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live) {
+int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live, bool raw) {
   const size_t n = live.size();
   std::vector<size_t> ll_off(n, 0);
   size_t ll_total = 0;
@@ -342,7 +344,7 @@ int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live) {
       DwtBandOut& o = a.band[g.comp][g.orient];
       o.first_block = live[i]->block_base + g.first_block;
       o.ncbx = std::max(g.ncbx, 1);
-      o.step = p.quants[g.quant].step_f32;
+      o.step = raw ? 0.0f : p.quants[g.quant].step_f32;
     }
     launch_dwt_level(a, p.lossless, c->stream);
     ++launches;
@@ -366,6 +368,9 @@ int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live) {
         int32_t* ll = dptr<int32_t>(c->ll0) + ll_off[i];
         const size_t half = p.levels >= 2 ? ll_plane_elems(p) : 0;
         DwtLevelArgs a = level_args(p, l, page_px(i), live[i]->block_base, coef, ll, ll + half);
+        if (raw)
+          for (auto& bc : a.band)
+            for (auto& bo : bc) bo.step = 0.0f;
         if (a.rw >= 2 && a.rh >= 2) {
           args.push_back(a);
           bases.push_back(g.ntiles);
@@ -443,6 +448,7 @@ int host_threads(jp2g_ctx* c) {
 // Debug captures of a single-page wave.
 struct WaveDebug {
   bool stop_after_dwt = false;
+  bool raw_coefficients = false;  // lossy: f32 coefficient bits instead of quantised indices
   std::vector<BlockOut>* res = nullptr;
 };
 
@@ -636,7 +642,7 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
     return kEncodeFailed;
   record(c, 1);
   // ---- colour + DWT + quantisation, one launch per level for the wave ----
-  if (int rc = run_dwt_wave(c, live)) return rc;
+  if (int rc = run_dwt_wave(c, live, dbg && dbg->raw_coefficients)) return rc;
   record(c, 2);
   if (dbg && dbg->stop_after_dwt) {
     if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "DWT")) return kEncodeFailed;
@@ -812,7 +818,7 @@ void release_pools(jp2g_ctx* c) {
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
                     &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
-                    &c->mqorder, &c->mqscratch};
+                    &c->mqorder, &c->mqscratch, &c->recon, &c->reconblk};
   for (DevBuf* b : bufs) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -1020,7 +1026,7 @@ void jp2g_destroy(jp2g_ctx* c) {
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
                     &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
-                    &c->mqorder, &c->mqscratch};
+                    &c->mqorder, &c->mqscratch, &c->recon, &c->reconblk};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   HostBuf* hb[] = {&c->hpx, &c->hpx2, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres, &c->hcount};
@@ -1077,6 +1083,87 @@ int jp2g_encode_device(jp2g_ctx* c, const uint8_t* d_px, uint32_t w, uint32_t h,
   j.quality = quality;
   j.format = format;
   int rc = encode_one(c, &j, nullptr);
+  return finish_output(c, rc, j.out, out, out_len);
+}
+
+// Quality metrics of the page the last wave encoded (a single-page wave
+// whose device buffers are still in place): compute_quality_metrics
+// (backend.rs:305-433) on the device. Lossless pages give +inf and 1.0.
+static int page_metrics(jp2g_ctx* c, const PageJob& j, double* psnr, double* ssim) {
+  const PagePlan& p = j.plan;
+  if (p.quality >= 100) {
+    *psnr = std::numeric_limits<double>::infinity();
+    *ssim = 1.0;
+    return kOk;
+  }
+  if (p.ncomp == 3 && !p.use_mct)
+    return set_err(c, kEncodeFailed, "quality metrics not implemented for this colorspace configuration");
+  std::vector<ReconBlock> rb(p.nblocks);
+  for (const BandGeom& g : p.bands)
+    for (int by = 0; by < g.ncby; ++by)
+      for (int bx = 0; bx < g.ncbx; ++bx) {
+        ReconBlock& r = rb[g.first_block + (uint32_t)(by * g.ncbx + bx)];
+        r.x0 = (uint32_t)(g.x0 + bx * p.cbw);
+        r.y0 = (uint32_t)(g.y0 + by * p.cbh);
+        r.comp = (uint32_t)g.comp;
+        r.step = p.quants[g.quant].step_f32;
+      }
+  const size_t n = (size_t)p.width * p.height;
+  if (!reserve(c, c->recon, (n * (p.ncomp + 3) + 64) * sizeof(float) + 16) ||
+      !reserve(c, c->reconblk, std::max<size_t>(rb.size(), 1) * sizeof(ReconBlock)) ||
+      !cuda_ok(c, cudaMemcpyAsync(c->reconblk.p, rb.data(), rb.size() * sizeof(ReconBlock), cudaMemcpyHostToDevice,
+                                  c->stream), "H2D metrics blocks"))
+    return kEncodeFailed;
+  ReconArgs r{};
+  r.blocks = dptr<BlockDesc>(c->blocks);
+  r.rblocks = dptr<ReconBlock>(c->reconblk);
+  r.keep = dptr<BlockKeep>(c->keep);
+  r.passes = dptr<PassRec>(c->passes);
+  r.coef = dptr<int32_t>(c->coef);
+  r.cbw = p.cbw;
+  r.cbh = p.cbh;
+  r.nblocks = p.nblocks;
+  r.width = p.width;
+  r.height = p.height;
+  r.ncomp = p.ncomp;
+  r.px = j.dev_px ? j.dev_px : dptr<uint8_t>(c->px) + j.px_off;
+  float* f = dptr<float>(c->recon);
+  r.stats = reinterpret_cast<double*>(f);  // 16 bytes at the start
+  r.plane = f + 4;
+  r.tmp = r.plane + n * p.ncomp;
+  r.luma_orig = r.tmp + n;
+  r.luma_dec = r.luma_orig + n;
+  launch_recon(r, p.ladder.data(), p.levels, c->stream);
+  double sums[2] = {0, 0};
+  if (!cuda_ok(c, cudaMemcpyAsync(sums, r.stats, sizeof sums, cudaMemcpyDeviceToHost, c->stream), "D2H metrics") ||
+      !cuda_ok(c, cudaStreamSynchronize(c->stream), "metrics kernels"))
+    return kEncodeFailed;
+  const double mse = sums[0] / (double)(n * (size_t)p.ncomp);
+  const double max_val = (double)((1u << p.precision) - 1);
+  *psnr = mse < 1e-10 ? 100.0 : 20.0 * std::log10(max_val / std::sqrt(mse));
+  const uint32_t nb8 = (p.width / 8) * (p.height / 8);
+  *ssim = nb8 == 0 ? 1.0 : sums[1] / (double)nb8;
+  return kOk;
+}
+
+int jp2g_encode_with_psnr(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, uint32_t ncomp, int interleaved,
+                          uint8_t quality, int format, uint8_t** out, size_t* out_len, double* psnr_db,
+                          double* ssim) {
+  if (!c) return JP2G_INVALID_INPUT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!out || !out_len || !psnr_db || !ssim) return set_err(c, JP2G_INVALID_INPUT, "output pointer is null");
+  if (!px) return set_err(c, JP2G_INVALID_INPUT, "pixel pointer is null");
+  cudaSetDevice(c->device);
+  PageJob j;
+  j.host_px = px;
+  j.w = w;
+  j.h = h;
+  j.ncomp = ncomp;
+  j.interleaved = interleaved;
+  j.quality = quality;
+  j.format = format;
+  int rc = encode_one(c, &j, nullptr);
+  if (rc == JP2G_OK) rc = page_metrics(c, j, psnr_db, ssim);
   return finish_output(c, rc, j.out, out, out_len);
 }
 
@@ -1508,8 +1595,22 @@ int jp2g_counters(jp2g_ctx* c, uint64_t* out, int n) {
   return k;
 }
 
+static int debug_coefficients(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, uint32_t ncomp,
+                              uint8_t quality, uint32_t comp, int32_t* plane, bool raw);
+
 int jp2g_debug_coefficients(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h,
                             uint32_t ncomp, uint8_t quality, uint32_t comp, int32_t* plane) {
+  return debug_coefficients(c, px, w, h, ncomp, quality, comp, plane, false);
+}
+
+int jp2g_debug_coefficients_f32(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, uint32_t ncomp,
+                                uint8_t quality, uint32_t comp, float* plane) {
+  if (c && quality >= 100) return set_err(c, JP2G_INVALID_INPUT, "f32 coefficients exist only for lossy qualities");
+  return debug_coefficients(c, px, w, h, ncomp, quality, comp, reinterpret_cast<int32_t*>(plane), true);
+}
+
+static int debug_coefficients(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, uint32_t ncomp,
+                              uint8_t quality, uint32_t comp, int32_t* plane, bool raw) {
   if (!c) return JP2G_INVALID_INPUT;
   std::lock_guard<std::mutex> lk(c->mu);
   if (!px || !plane) return set_err(c, JP2G_INVALID_INPUT, "null pointer");
@@ -1523,6 +1624,7 @@ int jp2g_debug_coefficients(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t
   j.quality = quality;
   WaveDebug dbg;
   dbg.stop_after_dwt = true;
+  dbg.raw_coefficients = raw;
   int rc = encode_one(c, &j, &dbg);
   if (rc) return rc;
   const PagePlan& p = j.plan;

@@ -56,7 +56,10 @@ __device__ __forceinline__ float lift97(float x, float c, float l, float r) {
 }
 
 __device__ __forceinline__ int32_t quantize(float v, float step) {
-  // src/simd/scalar.rs:100-106: trunc(v / step), saturating.
+  // src/simd/scalar.rs:100-106: trunc(v / step), saturating. Plan steps are
+  // floored at 1e-6 (backend.rs:602-620); a zero step asks for the
+  // unquantised coefficient's bits instead (jp2g_debug_coefficients_f32).
+  if (step == 0.0f) return __float_as_int(v);
   return __float2int_rz(__fdiv_rn(v, step));
 }
 

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "jp2g_internal.h"
 
 namespace jp2g {
@@ -112,6 +114,38 @@ struct PcrdArgs {
 };
 
 void launch_pcrd(const PcrdArgs& a, cudaStream_t st);
+
+// Where a code-block's samples sit in its component's plane (Mallat
+// layout), and its quantiser step.
+struct ReconBlock {
+  uint32_t x0, y0;
+  uint32_t comp;
+  float step;
+};
+
+// Reconstruction of one encoded page for its quality metrics (recon.cu).
+struct ReconArgs {
+  const BlockDesc* blocks;
+  const ReconBlock* rblocks;
+  const BlockKeep* keep;
+  const PassRec* passes;
+  const int32_t* coef;
+  int cbw, cbh;
+  uint32_t nblocks;
+  uint32_t width, height;
+  int ncomp;
+  const uint8_t* px;  // the page's interleaved pixels on the device
+  float* plane;       // ncomp planes of width * height
+  float* tmp;         // one plane of scratch
+  float* luma_orig;
+  float* luma_dec;
+  double* stats;      // [0] sum of squared errors, [1] sum of 8x8 block SSIMs
+};
+
+// Dequantisation of the retained bit-planes, inverse 9/7 per component
+// (ladder[0..levels], index 0 the smallest resolution), colour and the two
+// sums of the metrics.
+void launch_recon(const ReconArgs& r, const std::pair<int, int>* ladder, int levels, cudaStream_t st);
 
 // Packs the retained payload bytes of every block, in work-list order, into
 // `dst`; offsets[b] receives the byte offset of block b and offsets[n] the

@@ -86,6 +86,11 @@ void inv97_2d(float* data, int w, int h, int levels);
 
 // Quantised (9/7) or raw (5/3) coefficient plane of one component in the
 // reference's deinterleaved Mallat layout.
+// FP64 forward 9/7 of one component (unquantised, Mallat layout) and the
+// quantiser step of every coefficient position.
+std::vector<float> component_unquantized_f32(const Plan& p, const Planes& px, int comp, int threads);
+std::vector<double> component_coefficients_f64(const Plan& p, const Planes& px, int comp);
+std::vector<float> coefficient_steps(const Plan& p);
 std::vector<int32_t> component_coefficients(const Plan& p, const Planes& px,
                                             int comp, int threads);
 

@@ -136,6 +136,35 @@ int orc_reframe(const uint8_t* cs, size_t n, uint32_t w, uint32_t h, int ncomp, 
   }
 }
 
+// FP64 9/7 coefficients of one component (irreversible path, unquantised,
+// Mallat layout, W*H double), the quantiser step of each position (W*H
+// float) and, when f32_out is not null, the restatement's own f32
+// coefficients before quantisation, for measuring the f32 pipeline against
+// exact lifting.
+int orc_coefficients_f64(const uint8_t* px, uint32_t w, uint32_t h, int ncomp, int quality, int comp,
+                         double* out, float* steps, float* f32_out) {
+  if (int rc = check_input(w, h, ncomp)) return rc;
+  try {
+    orc::Plan p = orc::build_plan(w, h, ncomp, quality, 0);
+    if (p.lossless) {
+      g_err = "the FP64 9/7 path is for lossy qualities";
+      return orc::kInvalidInput;
+    }
+    orc::Planes planes = orc::planes_from_bytes(px, w, h, ncomp);
+    auto c = orc::component_coefficients_f64(p, planes, comp);
+    if (f32_out) {
+      auto f = orc::component_unquantized_f32(p, planes, comp, 1);
+      std::memcpy(f32_out, f.data(), f.size() * sizeof(float));
+    }
+    auto st = orc::coefficient_steps(p);
+    std::memcpy(out, c.data(), c.size() * sizeof(double));
+    std::memcpy(steps, st.data(), st.size() * sizeof(float));
+    return 0;
+  } catch (const orc::Error& e) {
+    return fail(e);
+  }
+}
+
 // Quantised coefficient plane of one component (Mallat layout, W*H int32).
 int orc_coefficients(const uint8_t* px, uint32_t w, uint32_t h, int ncomp,
                      int quality, int comp, int32_t* out) {

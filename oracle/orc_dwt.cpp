@@ -268,25 +268,7 @@ std::vector<int32_t> component_coefficients(const Plan& p, const Planes& px,
     fwd53_2d(d.data(), w, h, p.levels);
     return d;
   }
-  // irreversible_input_component (backend.rs:436-476)
-  std::vector<float> f(n);
-  if (!p.use_mct) {
-    for (size_t i = 0; i < n; ++i) f[i] = static_cast<float>(px[comp][i] - 128);
-  } else {
-    const auto &r = px[0], &g = px[1], &b = px[2];
-    for (size_t i = 0; i < n; ++i) {  // src/simd/scalar.rs:149-171
-      float rf = static_cast<float>(r[i] - 128);
-      float gf = static_cast<float>(g[i] - 128);
-      float bf = static_cast<float>(b[i] - 128);
-      if (comp == 0)
-        f[i] = 0.299f * rf + 0.587f * gf + 0.114f * bf;
-      else if (comp == 1)
-        f[i] = -0.16875f * rf + -0.33126f * gf + 0.5f * bf;
-      else
-        f[i] = 0.5f * rf - 0.41869f * gf - 0.08131f * bf;
-    }
-  }
-  fwd97_2d(f.data(), w, h, p.levels, threads);
+  std::vector<float> f = component_unquantized_f32(p, px, comp, threads);
   // quantize_97_coefficients (backend.rs:519-587)
   std::vector<int32_t> out(n, 0);
   auto res = resolutions(w, h, p.levels);
@@ -310,6 +292,116 @@ std::vector<int32_t> component_coefficients(const Plan& p, const Planes& px,
     rect(lo.first, lo.second, full.first, full.second, step_of(r, HH));
   }
   return out;
+}
+
+// The irreversible path before quantisation: level shift, ICT and the f32
+// 9/7 transform of one component.
+std::vector<float> component_unquantized_f32(const Plan& p, const Planes& px, int comp, int threads) {
+  const int w = p.width, h = p.height;
+  const size_t n = (size_t)w * h;
+  // irreversible_input_component (backend.rs:436-476)
+  std::vector<float> f(n);
+  if (!p.use_mct) {
+    for (size_t i = 0; i < n; ++i) f[i] = static_cast<float>(px[comp][i] - 128);
+  } else {
+    const auto &r = px[0], &g = px[1], &b = px[2];
+    for (size_t i = 0; i < n; ++i) {  // src/simd/scalar.rs:149-171
+      float rf = static_cast<float>(r[i] - 128);
+      float gf = static_cast<float>(g[i] - 128);
+      float bf = static_cast<float>(b[i] - 128);
+      if (comp == 0)
+        f[i] = 0.299f * rf + 0.587f * gf + 0.114f * bf;
+      else if (comp == 1)
+        f[i] = -0.16875f * rf + -0.33126f * gf + 0.5f * bf;
+      else
+        f[i] = 0.5f * rf - 0.41869f * gf - 0.08131f * bf;
+    }
+  }
+  fwd97_2d(f.data(), w, h, p.levels, threads);
+  return f;
+}
+
+// ------------------------------------------------------ FP64 lifting ------
+// The irreversible path of component_coefficients in double precision: the
+// level shift and ICT (src/simd/scalar.rs:135-171) and every 9/7 lifting step
+// and scaling (src/dwt/irrev97.rs:10-15, 92-129, 261-336) in the same order,
+// with the constants' decimal values as doubles. It measures how far the
+// reference's f32 pipeline is from exact lifting; quantised with the same
+// steps it gives the indices an f64 pipeline would code.
+static const double kAlpha64 = -1.586134342059924, kBeta64 = -0.052980118572961;
+static const double kGamma64 = 0.882911075530934, kDelta64 = 0.443506852043971;
+static const double kK64 = 1.230174104914001, kInvK64 = 1.0 / 1.230174104914001;
+
+static void lift64(double* x, int n, size_t stride, int parity, double c) {
+  for (int j = parity; j < n; j += 2) {
+    double l = x[(size_t)sym_index(n, j - 1) * stride];
+    double r = x[(size_t)sym_index(n, j + 1) * stride];
+    x[(size_t)j * stride] = x[(size_t)j * stride] + c * (l + r);
+  }
+}
+
+static void fwd97_1d_f64(double* x, int n, size_t stride, double* tmp) {
+  if (n < 2) {
+    if (n == 1) x[0] = x[0] * kInvK64;
+    return;
+  }
+  lift64(x, n, stride, 1, kAlpha64);
+  lift64(x, n, stride, 0, kBeta64);
+  lift64(x, n, stride, 1, kGamma64);
+  lift64(x, n, stride, 0, kDelta64);
+  for (int i = 0; i < n; i += 2) x[(size_t)i * stride] = x[(size_t)i * stride] * kInvK64;
+  for (int i = 1; i < n; i += 2) x[(size_t)i * stride] = x[(size_t)i * stride] * kK64;
+  int sn = (n + 1) / 2, dn = n - sn;
+  for (int i = 0; i < sn; ++i) tmp[i] = x[(size_t)(2 * i) * stride];
+  for (int i = 0; i < dn; ++i) tmp[sn + i] = x[(size_t)(2 * i + 1) * stride];
+  for (int i = 0; i < n; ++i) x[(size_t)i * stride] = tmp[i];
+}
+
+std::vector<double> component_coefficients_f64(const Plan& p, const Planes& px, int comp) {
+  const int w = p.width, h = p.height;
+  const size_t n = (size_t)w * h;
+  std::vector<double> f(n);
+  for (size_t i = 0; i < n; ++i) {
+    if (!p.use_mct) {
+      f[i] = (double)(px[comp][i] - 128);
+    } else {
+      const double r = px[0][i] - 128, g = px[1][i] - 128, b = px[2][i] - 128;
+      f[i] = comp == 0 ? 0.299 * r + 0.587 * g + 0.114 * b
+                       : comp == 1 ? -0.16875 * r + -0.33126 * g + 0.5 * b : 0.5 * r - 0.41869 * g - 0.08131 * b;
+    }
+  }
+  auto res = resolutions(w, h, p.levels);
+  std::vector<double> tmp(std::max(w, h));
+  for (int li = p.levels; li >= 1; --li) {
+    const int rw = res[li].first, rh = res[li].second;
+    for (int x = 0; x < rw; ++x) fwd97_1d_f64(f.data() + x, rh, w, tmp.data());
+    for (int y = 0; y < rh; ++y) fwd97_1d_f64(f.data() + (size_t)y * w, rw, 1, tmp.data());
+  }
+  return f;
+}
+
+// Quantiser step of every coefficient position of a plane (Mallat layout).
+std::vector<float> coefficient_steps(const Plan& p) {
+  const int w = p.width, h = p.height;
+  std::vector<float> st((size_t)w * h, 1.0f);
+  auto res = resolutions(w, h, p.levels);
+  auto step_of = [&](int r, Band b) {
+    for (const auto& q : p.quants)
+      if (q.resolution == r && q.band == b) return quant_step_f32(p.precision, b, q.exponent, q.mantissa);
+    throw Error(kEncodeFailed, "missing quantization parameters");
+  };
+  auto rect = [&](int x0, int y0, int x1, int y1, float step) {
+    for (int y = y0; y < y1; ++y)
+      for (int x = x0; x < x1; ++x) st[(size_t)y * w + x] = step;
+  };
+  rect(0, 0, res[0].first, res[0].second, step_of(0, LL));
+  for (int i = 0; i < p.levels; ++i) {
+    auto lo = res[i], full = res[i + 1];
+    rect(lo.first, 0, full.first, lo.second, step_of(i + 1, HL));
+    rect(0, lo.second, lo.first, full.second, step_of(i + 1, LH));
+    rect(lo.first, lo.second, full.first, full.second, step_of(i + 1, HH));
+  }
+  return st;
 }
 
 Planes planes_from_bytes(const uint8_t* px, uint32_t w, uint32_t h, int ncomp) {

@@ -68,6 +68,19 @@ class Oracle:
         self._err(rc, "orc_coefficients")
         return out.reshape(h, w)
 
+    def coefficients_f64(self, px, w, h, ncomp, quality, comp):
+        """(FP64 9/7 coefficients, quantiser steps, the f32 restatement's
+        unquantised coefficients) of one component, each h x w."""
+        px = np.ascontiguousarray(px, dtype=np.uint8)
+        c64 = np.zeros(w * h, np.float64)
+        st = np.zeros(w * h, np.float32)
+        f32 = np.zeros(w * h, np.float32)
+        ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        rc = self.lib.orc_coefficients_f64(ptr(px), ctypes.c_uint32(w), ctypes.c_uint32(h), ncomp, quality, comp,
+                                           ptr(c64), ptr(st), ptr(f32))
+        self._err(rc, "orc_coefficients_f64")
+        return c64.reshape(h, w), st.reshape(h, w), f32.reshape(h, w)
+
     def plan(self, w, h, ncomp, quality):
         lv, cbw, nq = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         q = np.zeros(4 * 32, np.int32)
