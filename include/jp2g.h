@@ -99,8 +99,8 @@ typedef struct jp2g_request {
 
 /* Encodes n pages. Pages are grouped into device waves that share one flat
  * code-block work list (colour+DWT per page, then Tier-1, PCRD and
- * compaction over all the wave's blocks in single launches); the host
- * Tier-2 of one wave overlaps the next wave's device work. Per page:
+ * compaction and Tier-2 over all the wave's blocks and packets in single
+ * launches; only the finished codestreams are read back). Per page:
  * outs[i]/out_lens[i] receive the codestream (free with jp2g_free) and
  * status[i] its status; one page's failure does not fail the others.
  * Returns JP2G_OK, or the first failing page's status (its message in
@@ -114,7 +114,7 @@ int jp2g_encode_batch(jp2g_ctx* ctx, const jp2g_request* reqs, uint32_t n, uint8
  * src/plan/validate.rs:4-62, before any device work) and queues it; a
  * worker thread admits queued requests into the next device wave as the
  * previous one leaves the device, up to JP2G_OPT_WAVE_BLOCKS code-blocks,
- * while a second thread writes the codestreams of finished waves. The pixel
+ * and a second thread completes the finished waves' tickets. The pixel
  * buffer must stay valid until jp2g_poll has returned the ticket's result.
  * jp2g_poll waits up to timeout_ms (< 0: no limit) and returns the
  * request's status with its codestream, or JP2G_PENDING if it is not done
@@ -206,8 +206,10 @@ void* jp2g_stream(jp2g_ctx* ctx);
  * device stages summed over its waves, [6] the host time outside them and
  * [7] the wall time of the call):
  * [0] h2d, [1] dwt (all levels), [2] tier-1, [3] pcrd, [4] compaction,
- * [5] d2h, [6] host tier-2 + codestream, [7] total, and the tier-1 split
- * [8] analysis, [9] context modelling, [10] MQ coding. Returns the count. */
+ * [5] read-back of the codestreams into the callers' buffers, [6] host
+ * time after it, [7] total, the tier-1 split [8] analysis and bit-plane
+ * masks, [9] context modelling, [10] MQ coding, and [11] device Tier-2
+ * (packet headers and assembly, between [4] and [5]). Returns the count. */
 int jp2g_set_timing(jp2g_ctx* ctx, int enabled);
 int jp2g_stage_times(jp2g_ctx* ctx, float* ms, int n);
 
@@ -233,7 +235,8 @@ int jp2g_debug_coefficients_f32(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, ui
 int jp2g_debug_blocks(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,
                       uint32_t ncomp, uint8_t quality, int32_t* rows, uint32_t cap,
                       uint32_t* nblocks);
-/* Host Tier-2 alone (no context, no device): packet headers, markers and
+/* Host Tier-2 alone (no context, no device; the encoder itself runs Tier-2
+ * on the device): packet headers, markers and
  * JP2 boxes of a w x h page whose nblocks code-blocks, in codestream order
  * (resolution, component, band, raster), retain npasses[i] passes in one
  * segment of seg_len[i] bytes, consecutive in `body`, above zbp[i] zero
@@ -241,6 +244,13 @@ int jp2g_debug_blocks(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t h,
 int jp2g_debug_assemble(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int format,
                         const uint16_t* npasses, const uint8_t* zbp, const uint32_t* seg_len,
                         const uint8_t* body, uint32_t nblocks, uint8_t** out, size_t* out_len);
+/* Device Tier-2 alone, on the same inputs as jp2g_debug_assemble: the
+ * per-block records and bodies go to the device and the packet headers,
+ * markers and JP2 boxes are written there (the kernels the encoder runs),
+ * so tests can compare the two assemblers byte for byte. */
+int jp2g_debug_assemble_device(jp2g_ctx* ctx, uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality,
+                               int format, const uint16_t* npasses, const uint8_t* zbp, const uint32_t* seg_len,
+                               const uint8_t* body, uint32_t nblocks, uint8_t** out, size_t* out_len);
 /* Encoding plan alone (no context, no device), as EncodingPlan::build makes
  * it (src/plan/mod.rs:116-177): decomposition levels, code-block width,
  * quantiser entries (up to 32, as (resolution, band, exponent, mantissa)),

@@ -52,7 +52,7 @@ EXPORTS = [
     "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
     "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
     "jp2g_autotune", "jp2g_debug_assemble", "jp2g_debug_plan", "jp2g_cancel", "jp2g_debug_context_labels",
-    "jp2g_debug_coefficients_f32", "jp2g_encode_with_psnr",
+    "jp2g_debug_coefficients_f32", "jp2g_encode_with_psnr", "jp2g_debug_assemble_device",
 ]
 
 PENDING = 6
@@ -136,6 +136,7 @@ def load_library(path: str = LIB_PATH):
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(_u8p),
                                             ctypes.POINTER(ctypes.c_size_t)]
+        lib.jp2g_debug_assemble_device.argtypes = [ctypes.c_void_p] + lib.jp2g_debug_assemble.argtypes
         _lib = lib
         return lib
 
@@ -301,6 +302,26 @@ class Engine:
             self._inflight.pop(ticket, None)
         return True
 
+    def debug_assemble_device(self, w: int, h: int, ncomp: int, quality: int, fmt: int, npasses, zbp, seg_len,
+                              body) -> bytes:
+        """Device Tier-2 alone on the inputs of debug_assemble()."""
+        npasses = np.ascontiguousarray(npasses, dtype=np.uint16)
+        zbp = np.ascontiguousarray(zbp, dtype=np.uint8)
+        seg_len = np.ascontiguousarray(seg_len, dtype=np.uint32)
+        body = np.ascontiguousarray(np.frombuffer(bytes(body), np.uint8) if not isinstance(body, np.ndarray)
+                                    else body, dtype=np.uint8)
+        out = _u8p()
+        n = ctypes.c_size_t()
+        ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        with self._lock:
+            rc = self.lib.jp2g_debug_assemble_device(self.handle, w, h, ncomp, quality, fmt, ptr(npasses), ptr(zbp),
+                                                     ptr(seg_len), ptr(body) if body.size else None, len(npasses),
+                                                     ctypes.byref(out), ctypes.byref(n))
+            self._check(rc)
+        data = ctypes.string_at(out, n.value)
+        self.lib.jp2g_free(out)
+        return data
+
     def set_option(self, option: int, value: int):
         self._check(self.lib.jp2g_set_option(self.handle, option, value))
 
@@ -332,10 +353,10 @@ class Engine:
         self.lib.jp2g_set_timing(self.handle, int(on))
 
     def stage_times(self):
-        ms = (ctypes.c_float * 11)()
-        self.lib.jp2g_stage_times(self.handle, ms, 11)
-        keys = ["h2d", "dwt", "tier1", "pcrd", "compact", "d2h", "host_t2", "total",
-                "t1_analyze", "t1_model", "t1_mq"]
+        ms = (ctypes.c_float * 12)()
+        self.lib.jp2g_stage_times(self.handle, ms, 12)
+        keys = ["h2d", "dwt", "tier1", "pcrd", "compact", "d2h", "host", "total",
+                "t1_analyze", "t1_model", "t1_mq", "tier2"]
         return dict(zip(keys, list(ms)))
 
     def counters(self):

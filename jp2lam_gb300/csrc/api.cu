@@ -2,10 +2,10 @@
 //
 // jp2g_encode follows jp2lam::encode (src/encode/mod.rs:84-101): plan on the
 // host, then on the device colour+DWT+quantisation (one launch per level),
-// Tier-1 (one warp per code-block over the flat work list), PCRD (hull +
-// lambda selection) and compaction of the retained bytes; the per-block
-// retained table and the packed bytes come back to the host, which writes
-// the packet headers, markers and JP2 boxes.
+// Tier-1 (bit-plane masks, modelling, MQ over the flat work list), PCRD
+// (hull + lambda selection), compaction of the retained bytes and Tier-2
+// (packet headers, markers, JP2 boxes and the codestream itself); only the
+// finished codestreams come back to the host.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,6 +33,8 @@ bool init_t1_tables();
 void build_t1_tables(uint8_t* zc, uint8_t* sc, uint8_t* spb, uint32_t* mq);
 bool assemble_codestream(const PagePlan& p, const BlockKeep* keep, const uint8_t* body,
                          const uint32_t* offsets, std::vector<uint8_t>* out, Failure* err);
+bool codestream_prefix(const PagePlan& p, uint64_t payload, std::vector<uint8_t>* out, uint32_t* psot_pos,
+                       uint32_t* jp2c_pos, Failure* err);
 double norm97(int level, int orient);
 void context_labels_from_logic(uint8_t* zc, uint8_t* sc, uint8_t* spb);
 }  // namespace jp2g
@@ -54,7 +56,7 @@ struct HostBuf {
 };
 
 enum Stage { kH2D = 0, kDWT, kT1, kPCRD, kCompact, kD2H, kHost, kTotal, kNumStages };
-enum SubEvent { kEvAnalyzeEnd = kNumStages + 1, kEvModelEnd, kNumEvents };
+enum SubEvent { kEvAnalyzeEnd = kNumStages + 1, kEvModelEnd, kEvT2End, kNumEvents };
 
 // One page of a wave: its request, its plan and, after the device phase,
 // the page-local retained blocks and bytes that Tier-2 needs.
@@ -69,11 +71,17 @@ struct PageJob {
   uint32_t block_base = 0;  // the page's first code-block in the wave
   size_t px_off = 0;        // the page's pixels in the wave's staging buffer
   bool staged = false;      // copied to the device from pinned staging
-  std::vector<BlockKeep> keep;
-  std::vector<uint32_t> offsets;  // nblocks + 1 body offsets
-  std::vector<uint8_t> body;
-  const uint8_t* body_view = nullptr;  // the body in the host result buffer, when not copied
-  std::vector<uint8_t> out;       // the codestream (J2K or JP2)
+  uint8_t* cs = nullptr;  // the finished codestream (J2K or JP2), malloc'd
+  size_t cs_len = 0;
+  PageJob() = default;
+  PageJob(const PageJob&) = delete;
+  PageJob& operator=(const PageJob&) = delete;
+  ~PageJob() { std::free(cs); }
+  void drop_output() {
+    std::free(cs);
+    cs = nullptr;
+    cs_len = 0;
+  }
 };
 
 // A submitted request and, once done, its result.
@@ -100,17 +108,17 @@ struct jp2g_ctx {
   // device pools
   DevBuf px, ll0, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
       hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, planes, signs, sym, stats,
-      dwtargs, dwtbases, mqorder, mqscratch, recon, reconblk;
+      dwtargs, dwtbases, mqorder, mqscratch, recon, reconblk, t2pk, t2bd, t2pg, t2tmpl, t2tree, t2raw, t2hdr,
+      t2hdrlen, t2pktoff, t2pagelen, t2pageoff, t2out;
   // pinned host staging
-  HostBuf hpx, hpx2, hkeep, hoffsets, hbody, hres, hcount;
+  HostBuf hpx, hpx2, hkeep, hres, hcount, hpageoff, hout;
   bool timing = false;
   cudaEvent_t ev[kNumEvents] = {};
-  float stage_ms[kNumStages + 3] = {};
+  float stage_ms[kNumStages + 4] = {};
   uint64_t counters[8] = {};
   int64_t opt[JP2G_NUM_OPTS] = {160000, 0, 0, 0, 0, 0, 0};
-  // submit/poll: a worker thread forms waves from the queue and runs their
-  // device phase; a finisher thread runs Tier-2 of finished waves, so the
-  // next wave's device work overlaps the previous wave's host work.
+  // submit/poll: a worker thread forms waves from the queue and runs them;
+  // a finisher thread marks the finished waves' tickets done.
   std::mutex qmu;
   std::condition_variable qcv, fcv, dcv;
   std::deque<std::shared_ptr<Ticket>> pending;
@@ -450,6 +458,7 @@ struct WaveDebug {
   bool stop_after_dwt = false;
   bool raw_coefficients = false;  // lossy: f32 coefficient bits instead of quantised indices
   std::vector<BlockOut>* res = nullptr;
+  std::vector<BlockKeep>* keep = nullptr;  // the retained-pass table
 };
 
 // Pixels of a wave's host-memory pages, staged in pinned memory.
@@ -531,6 +540,164 @@ size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
   return total;
 }
 
+// Nodes of a tag tree over w x h leaves (ISO/IEC 15444-1 B.10.2): every
+// level down to a single root.
+uint64_t tag_tree_nodes(int w, int h) {
+  if (w <= 0 || h <= 0) return 0;
+  uint64_t total = 0;
+  for (;;) {
+    total += (uint64_t)w * h;
+    if (w * h <= 1) return total;
+    w = (w + 1) / 2;
+    h = (h + 1) / 2;
+  }
+}
+
+// Tier-2 of the wave's pages on the device (t2dev.cu): the packet, band and
+// page tables and each page's marker prefix are made on the host from the
+// plans; the header and assembly kernels write the finished codestreams into
+// one device buffer; only those bytes come back, into pinned memory, and from
+// there into each page's own malloc'd buffer. Pages already failed are
+// skipped.
+int run_tier2(jp2g_ctx* c, const std::vector<PageJob*>& live, const BlockKeep* d_keep,
+              const uint32_t* d_offsets, const uint8_t* d_body, uint32_t body_total) {
+  std::vector<T2Packet> pks;
+  std::vector<T2Band> bds;
+  std::vector<T2Page> pgs;
+  std::vector<uint8_t> tmpl;
+  std::vector<PageJob*> pages;
+  uint64_t tree_nodes = 0, raw_words = 0, hdr_bytes = 0;
+  for (PageJob* j : live) {
+    if (j->status != kOk) continue;
+    const PagePlan& p = j->plan;
+    T2Page pg{};
+    pg.packet0 = (uint32_t)pks.size();
+    pg.tmpl_off = (uint32_t)tmpl.size();
+    std::vector<uint8_t> pre;
+    Failure f{};
+    if (!codestream_prefix(p, 0, &pre, &pg.psot_pos, &pg.jp2c_pos, &f)) {
+      j->status = f.code;
+      j->err = f.msg;
+      continue;
+    }
+    tmpl.insert(tmpl.end(), pre.begin(), pre.end());
+    pg.tmpl_len = (uint32_t)pre.size();
+    // bands are stored res -> comp -> orient: a packet is a run of one
+    // (resolution, component)
+    size_t bi = 0;
+    while (bi < p.bands.size()) {
+      size_t be = bi;
+      while (be < p.bands.size() && p.bands[be].res == p.bands[bi].res && p.bands[be].comp == p.bands[bi].comp)
+        ++be;
+      T2Packet pk{};
+      pk.band0 = (uint32_t)bds.size();
+      pk.nbands = (uint32_t)(be - bi);
+      pk.page = (uint32_t)pgs.size();
+      uint64_t nblk = 0;
+      for (size_t k = bi; k < be; ++k) {
+        const BandGeom& g = p.bands[k];
+        T2Band b{};
+        b.first_block = j->block_base + g.first_block;
+        b.tree_off = (uint32_t)tree_nodes;
+        b.ncbx = (uint16_t)g.ncbx;
+        b.ncby = (uint16_t)g.ncby;
+        bds.push_back(b);
+        tree_nodes += tag_tree_nodes(g.ncbx, g.ncby);
+        nblk += (uint64_t)g.ncbx * g.ncby;
+      }
+      const BandGeom& last = p.bands[be - 1];
+      pk.b0 = j->block_base + p.bands[bi].first_block;
+      pk.b1 = j->block_base + last.first_block + (uint32_t)(last.ncbx * last.ncby);
+      // header bounds per code-block: 400 unstuffed bits (inclusion and
+      // zero bit-plane tree bits, Table B-4 code, Lblock comma and length),
+      // 60 stuffed bytes
+      pk.raw_off = (uint32_t)raw_words;
+      raw_words += (1 + 400 * nblk) / 32 + 2;
+      pk.hdr_off = (uint32_t)hdr_bytes;
+      hdr_bytes += 60 * nblk + 16;
+      pks.push_back(pk);
+      bi = be;
+    }
+    pg.npackets = (uint32_t)pks.size() - pg.packet0;
+    pgs.push_back(pg);
+    pages.push_back(j);
+  }
+  if (pgs.empty()) return kOk;
+  const uint64_t out_bound = tmpl.size() + hdr_bytes + body_total + 2 * pgs.size();
+  if (out_bound > 0xffffffffull || raw_words > 0xffffffffull)
+    return set_err(c, kUnsupportedFeature, "codestreams of one device wave exceed 4 GiB");
+  const uint32_t npk = (uint32_t)pks.size(), npg = (uint32_t)pgs.size();
+  if (!reserve(c, c->t2pk, npk * sizeof(T2Packet)) || !reserve(c, c->t2bd, bds.size() * sizeof(T2Band)) ||
+      !reserve(c, c->t2pg, npg * sizeof(T2Page)) || !reserve(c, c->t2tmpl, tmpl.size()) ||
+      !reserve(c, c->t2tree, std::max<uint64_t>(tree_nodes, 1) * sizeof(T2Node)) ||
+      !reserve(c, c->t2raw, (raw_words + 2) * 4) || !reserve(c, c->t2hdr, hdr_bytes) ||
+      !reserve(c, c->t2hdrlen, npk * 4) || !reserve(c, c->t2pktoff, npk * 4) || !reserve(c, c->t2pagelen, npg * 4) ||
+      !reserve(c, c->t2pageoff, (npg + 1) * 4) || !reserve(c, c->t2out, out_bound) ||
+      !reserve(c, c->scratch, ((size_t)npg / 1024 + 2) * 4) ||
+      !reserve_host(c, c->hpageoff, (npg + 1) * 4))
+    return kEncodeFailed;
+  if (!cuda_ok(c, cudaMemcpyAsync(c->t2pk.p, pks.data(), npk * sizeof(T2Packet), cudaMemcpyHostToDevice, c->stream),
+               "H2D packets") ||
+      !cuda_ok(c, cudaMemcpyAsync(c->t2bd.p, bds.data(), bds.size() * sizeof(T2Band), cudaMemcpyHostToDevice,
+                                  c->stream), "H2D bands") ||
+      !cuda_ok(c, cudaMemcpyAsync(c->t2pg.p, pgs.data(), npg * sizeof(T2Page), cudaMemcpyHostToDevice, c->stream),
+               "H2D pages") ||
+      !cuda_ok(c, cudaMemcpyAsync(c->t2tmpl.p, tmpl.data(), tmpl.size(), cudaMemcpyHostToDevice, c->stream),
+               "H2D marker prefixes") ||
+      !cuda_ok(c, cudaMemsetAsync(c->t2raw.p, 0, (raw_words + 2) * 4, c->stream), "memset"))
+    return kEncodeFailed;
+  T2Args a{};
+  a.packets = dptr<T2Packet>(c->t2pk);
+  a.npackets = npk;
+  a.bands = dptr<T2Band>(c->t2bd);
+  a.pages = dptr<T2Page>(c->t2pg);
+  a.npages = npg;
+  a.keep = d_keep;
+  a.offsets = d_offsets;
+  a.body = d_body;
+  a.tmpl = dptr<uint8_t>(c->t2tmpl);
+  a.tree = dptr<T2Node>(c->t2tree);
+  a.raw = dptr<uint32_t>(c->t2raw);
+  a.hdr = dptr<uint8_t>(c->t2hdr);
+  a.hdr_len = dptr<uint32_t>(c->t2hdrlen);
+  a.pkt_off = dptr<uint32_t>(c->t2pktoff);
+  a.page_len = dptr<uint32_t>(c->t2pagelen);
+  a.page_off = dptr<uint32_t>(c->t2pageoff);
+  a.out = dptr<uint8_t>(c->t2out);
+  launch_t2(a, dptr<uint32_t>(c->scratch), c->stream);
+  c->counters[5] += 3 + (npg > 1024 ? 1 : 0);
+  record(c, kEvT2End);
+  const uint32_t* hoff = reinterpret_cast<const uint32_t*>(c->hpageoff.p);
+  if (!cuda_ok(c, cudaMemcpyAsync(c->hpageoff.p, a.page_off, (npg + 1) * 4, cudaMemcpyDeviceToHost, c->stream),
+               "D2H page offsets") ||
+      !cuda_ok(c, cudaStreamSynchronize(c->stream), "tier-2 kernels"))
+    return kEncodeFailed;
+  const uint32_t total = hoff[npg];
+  if (!reserve_host(c, c->hout, std::max<size_t>(total, 1)) ||
+      !cuda_ok(c, cudaMemcpyAsync(c->hout.p, a.out, total, cudaMemcpyDeviceToHost, c->stream), "D2H codestreams") ||
+      !cuda_ok(c, cudaStreamSynchronize(c->stream), "D2H codestreams"))
+    return kEncodeFailed;
+  const uint8_t* hout = reinterpret_cast<const uint8_t*>(c->hout.p);
+  std::atomic<bool> oom{false};
+  auto take = [&](size_t i) {
+    PageJob* j = pages[i];
+    const size_t len = hoff[i + 1] - hoff[i];
+    j->drop_output();
+    j->cs = static_cast<uint8_t*>(std::malloc(std::max<size_t>(len, 1)));
+    if (!j->cs) {
+      oom = true;
+      j->status = kEncodeFailed;
+      j->err = "out of host memory";
+      return;
+    }
+    std::memcpy(j->cs, hout + hoff[i], len);
+    j->cs_len = len;
+  };
+  parallel_for(pages.size(), pages.size() >= 8 && total >= (8u << 20) ? host_threads(c) : 1, take);
+  (void)oom;
+  return kOk;
+}
+
 // Device phase of a wave of pages: plans and validation, inputs,
 // colour+DWT+quantisation per page, then Tier-1, PCRD and compaction over
 // the wave's flat code-block list (all pages' blocks, page after page), and
@@ -538,10 +705,8 @@ size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
 // that fails validation or overflows a block slot is marked and the rest
 // carry on; a CUDA failure fails the wave (return code). `pre`: the wave's
 // host pixels already staged by stage_pixels (else they are staged here).
-// borrow_body: the pages' bodies stay in the host result buffer (the caller
-// assembles them before the next wave reuses it) instead of being copied.
 int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
-             const Prestaged* pre = nullptr, bool borrow_body = false) {
+             const Prestaged* pre = nullptr) {
   std::memset(c->counters, 0, sizeof c->counters);
   std::vector<PageJob*> live;
   int cbw = 0;
@@ -743,33 +908,23 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
                  dptr<uint32_t>(c->scratch), c->stream);
   c->counters[5] += 3 + (nb > 1024 ? 1 : 0);  // 2 PCRD, scan + copy kernels
   record(c, 5);
-  // ---- read back ----
+  // ---- read back the per-block results ----
   if (!reserve_host(c, c->hkeep, std::max<size_t>(nb, 1) * sizeof(BlockKeep)) ||
-      !reserve_host(c, c->hres, std::max<size_t>(nb, 1) * sizeof(BlockOut)) ||
-      !reserve_host(c, c->hoffsets, (size_t)(nb + 1) * 4))
+      !reserve_host(c, c->hres, std::max<size_t>(nb, 1) * sizeof(BlockOut)))
     return kEncodeFailed;
+  uint32_t* hcount = reinterpret_cast<uint32_t*>(c->hcount.p);
   if (!cuda_ok(c, cudaMemcpyAsync(c->hkeep.p, c->keep.p, nb * sizeof(BlockKeep),
                                   cudaMemcpyDeviceToHost, c->stream), "D2H keep") ||
-      !cuda_ok(c, cudaMemcpyAsync(c->hoffsets.p, c->offsets.p, (size_t)(nb + 1) * 4,
-                                  cudaMemcpyDeviceToHost, c->stream), "D2H offsets") ||
       !cuda_ok(c, cudaMemcpyAsync(c->hres.p, c->res.p, nb * sizeof(BlockOut),
                                   cudaMemcpyDeviceToHost, c->stream), "D2H results") ||
-      !cuda_ok(c, cudaMemcpyAsync(reinterpret_cast<uint8_t*>(c->hcount.p) + 8, c->stats.p, 8,
-                                  cudaMemcpyDeviceToHost, c->stream), "D2H statistics") ||
+      !cuda_ok(c, cudaMemcpyAsync(hcount + 2, c->stats.p, 8, cudaMemcpyDeviceToHost, c->stream),
+               "D2H statistics") ||
+      !cuda_ok(c, cudaMemcpyAsync(hcount + 4, dptr<uint32_t>(c->offsets) + nb, 4, cudaMemcpyDeviceToHost,
+                                  c->stream), "D2H retained bytes") ||
       !cuda_ok(c, cudaStreamSynchronize(c->stream), "encode kernels"))
     return kEncodeFailed;
   const BlockKeep* hk = reinterpret_cast<const BlockKeep*>(c->hkeep.p);
-  const uint32_t* hoff = reinterpret_cast<const uint32_t*>(c->hoffsets.p);
-  const uint32_t total = hoff[nb];
-  if (!reserve_host(c, c->hbody, std::max<size_t>(total, 1))) return kEncodeFailed;
-  if (total > 0 &&
-      !cuda_ok(c, cudaMemcpyAsync(c->hbody.p, c->body.p, total, cudaMemcpyDeviceToHost, c->stream),
-               "D2H body"))
-    return kEncodeFailed;
-  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "D2H")) return kEncodeFailed;
-  record(c, 6);
-  // ---- each page's share, rebased to the page ----
-  const uint8_t* hbody = reinterpret_cast<const uint8_t*>(c->hbody.p);
+  const uint32_t total = hcount[4];
   for (PageJob* j : live) {
     const uint32_t b0 = j->block_base, n = j->plan.nblocks;
     for (uint32_t i = 0; i < n; ++i) {
@@ -784,18 +939,10 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
         break;
       }
     }
-    if (j->status != kOk) continue;
-    j->keep.assign(hk + b0, hk + b0 + n);
-    j->offsets.resize((size_t)n + 1);
-    for (uint32_t i = 0; i <= n; ++i) j->offsets[i] = hoff[b0 + i] - hoff[b0];
-    if (borrow_body) {
-      j->body.clear();
-      j->body_view = hbody + hoff[b0];
-    } else {
-      j->body.assign(hbody + hoff[b0], hbody + hoff[b0 + n]);
-      j->body_view = nullptr;
-    }
   }
+  // ---- Tier-2 and codestream assembly on the device ----
+  if (int rc = run_tier2(c, live, pa.keep, dptr<uint32_t>(c->offsets), dptr<uint8_t>(c->body), total)) return rc;
+  record(c, 6);
   const BlockOut* hr = reinterpret_cast<const BlockOut*>(c->hres.p);
   c->counters[0] = nb;
   for (uint32_t i = 0; i < nb; ++i) {
@@ -805,8 +952,9 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
     c->counters[6] += (uint64_t)hr[i].mbp * blocks[i].w * blocks[i].h;
   }
   c->counters[4] = total;
-  c->counters[7] = *reinterpret_cast<const uint64_t*>(reinterpret_cast<const uint8_t*>(c->hcount.p) + 8);
+  c->counters[7] = *reinterpret_cast<const uint64_t*>(hcount + 2);
   if (dbg && dbg->res) dbg->res->assign(hr, hr + nb);
+  if (dbg && dbg->keep) dbg->keep->assign(hk, hk + nb);
   return kOk;
 }
 
@@ -818,7 +966,9 @@ void release_pools(jp2g_ctx* c) {
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
                     &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
-                    &c->mqorder, &c->mqscratch, &c->recon, &c->reconblk};
+                    &c->mqorder, &c->mqscratch, &c->recon, &c->reconblk, &c->t2pk, &c->t2bd, &c->t2pg,
+                    &c->t2tmpl, &c->t2tree, &c->t2raw, &c->t2hdr, &c->t2hdrlen, &c->t2pktoff, &c->t2pagelen,
+                    &c->t2pageoff, &c->t2out};
   for (DevBuf* b : bufs) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -862,18 +1012,13 @@ int run_wave_within_budget(jp2g_ctx* c, PageJob* const* jobs, size_t n, const Pr
   return kOk;
 }
 
-// Host phase of one page: Tier-2 packet headers, markers and JP2 boxes.
-void finish_page(PageJob* j) {
-  if (j->status != kOk) return;
-  Failure f{};
-  const uint8_t* body = j->body_view ? j->body_view : j->body.data();
-  if (!assemble_codestream(j->plan, j->keep.data(), body, j->offsets.data(), &j->out, &f)) {
-    j->status = f.code;
-    j->err = f.msg;
-  }
-  j->body.clear();
-  j->body.shrink_to_fit();
-  j->body_view = nullptr;
+// Device Tier-2 (compaction end -> kEvT2End) is reported on its own; the
+// read-back stage then runs from kEvT2End to event 6.
+float stage_span(jp2g_ctx* c, int s) {
+  float ms = 0;
+  if (s == kD2H) cudaEventElapsedTime(&ms, c->ev[kEvT2End], c->ev[6]);
+  else cudaEventElapsedTime(&ms, c->ev[s], c->ev[s + 1]);
+  return ms;
 }
 
 // Adds the device stages of the wave just run (events 0..6) to stage_ms.
@@ -881,10 +1026,9 @@ void add_wave_stage_times(jp2g_ctx* c) {
   if (!c->timing) return;
   cudaEventSynchronize(c->ev[6]);
   float ms = 0;
-  for (int s = 0; s < kHost; ++s) {
-    cudaEventElapsedTime(&ms, c->ev[s], c->ev[s + 1]);
-    c->stage_ms[s] += ms;
-  }
+  for (int s = 0; s < kHost; ++s) c->stage_ms[s] += stage_span(c, s);
+  cudaEventElapsedTime(&ms, c->ev[kCompact + 1], c->ev[kEvT2End]);
+  c->stage_ms[kNumStages + 3] += ms;
   cudaEventElapsedTime(&ms, c->ev[0], c->ev[6]);
   c->stage_ms[kTotal] += ms;
   const int sub[3][2] = {{2, kEvAnalyzeEnd}, {kEvAnalyzeEnd, kEvModelEnd}, {kEvModelEnd, 3}};
@@ -898,8 +1042,9 @@ void add_wave_stage_times(jp2g_ctx* c) {
 void read_stage_times(jp2g_ctx* c) {
   if (!c->timing) return;
   cudaEventSynchronize(c->ev[8]);
-  for (int s = 0; s < kTotal; ++s) cudaEventElapsedTime(&c->stage_ms[s], c->ev[s], c->ev[s + 1]);
+  for (int s = 0; s < kTotal; ++s) c->stage_ms[s] = stage_span(c, s);
   cudaEventElapsedTime(&c->stage_ms[kTotal], c->ev[0], c->ev[8]);
+  cudaEventElapsedTime(&c->stage_ms[kNumStages + 3], c->ev[kCompact + 1], c->ev[kEvT2End]);
   // tier-1 split: analysis (+item list), modelling, MQ coding
   cudaEventElapsedTime(&c->stage_ms[kNumStages + 0], c->ev[2], c->ev[kEvAnalyzeEnd]);
   cudaEventElapsedTime(&c->stage_ms[kNumStages + 1], c->ev[kEvAnalyzeEnd], c->ev[kEvModelEnd]);
@@ -911,16 +1056,15 @@ void read_stage_times(jp2g_ctx* c) {
 int encode_one(jp2g_ctx* c, PageJob* j, WaveDebug* dbg) {
   PageJob* jobs[1] = {j};
   c->budget_hit = false;
-  int rc = run_wave(c, jobs, 1, dbg, nullptr, true);
+  int rc = run_wave(c, jobs, 1, dbg, nullptr);
   if (rc != kOk && c->budget_hit) {  // pools of earlier waves crowd the budget: retry from empty pools
     release_pools(c);
     c->budget_hit = false;
-    rc = run_wave(c, jobs, 1, dbg, nullptr, true);
+    rc = run_wave(c, jobs, 1, dbg, nullptr);
   }
   if (rc) return rc;
   if (j->status != kOk) return set_err(c, j->status, j->err);
   if (dbg && dbg->stop_after_dwt) return kOk;
-  finish_page(j);
   record(c, 7);
   record(c, 8);
   read_stage_times(c);
@@ -1026,10 +1170,12 @@ void jp2g_destroy(jp2g_ctx* c) {
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
                     &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
-                    &c->mqorder, &c->mqscratch, &c->recon, &c->reconblk};
+                    &c->mqorder, &c->mqscratch, &c->recon, &c->reconblk, &c->t2pk, &c->t2bd, &c->t2pg,
+                    &c->t2tmpl, &c->t2tree, &c->t2raw, &c->t2hdr, &c->t2hdrlen, &c->t2pktoff, &c->t2pagelen,
+                    &c->t2pageoff, &c->t2out};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
-  HostBuf* hb[] = {&c->hpx, &c->hpx2, &c->hkeep, &c->hoffsets, &c->hbody, &c->hres, &c->hcount};
+  HostBuf* hb[] = {&c->hpx, &c->hpx2, &c->hkeep, &c->hres, &c->hcount, &c->hpageoff, &c->hout};
   for (HostBuf* b : hb)
     if (b->p) cudaFreeHost(b->p);
   for (auto& ev : c->ev)
@@ -1038,14 +1184,15 @@ void jp2g_destroy(jp2g_ctx* c) {
   delete c;
 }
 
-static int finish_output(jp2g_ctx* c, int rc, std::vector<uint8_t>& bytes, uint8_t** out,
-                         size_t* out_len) {
+// Hands the page's codestream (already in its own malloc'd buffer) to the
+// caller.
+static int finish_output(jp2g_ctx* c, int rc, PageJob& j, uint8_t** out, size_t* out_len) {
   if (rc != JP2G_OK) return rc;
-  uint8_t* p = static_cast<uint8_t*>(std::malloc(std::max<size_t>(bytes.size(), 1)));
-  if (!p) return set_err(c, JP2G_ENCODE_FAILED, "out of host memory");
-  std::memcpy(p, bytes.data(), bytes.size());
-  *out = p;
-  *out_len = bytes.size();
+  if (!j.cs) return set_err(c, JP2G_ENCODE_FAILED, "no codestream was produced");
+  *out = j.cs;
+  *out_len = j.cs_len;
+  j.cs = nullptr;
+  j.cs_len = 0;
   return JP2G_OK;
 }
 
@@ -1065,7 +1212,7 @@ int jp2g_encode(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, uint32_t
   j.quality = quality;
   j.format = format;
   int rc = encode_one(c, &j, nullptr);
-  return finish_output(c, rc, j.out, out, out_len);
+  return finish_output(c, rc, j, out, out_len);
 }
 
 int jp2g_encode_device(jp2g_ctx* c, const uint8_t* d_px, uint32_t w, uint32_t h, uint32_t ncomp,
@@ -1083,7 +1230,7 @@ int jp2g_encode_device(jp2g_ctx* c, const uint8_t* d_px, uint32_t w, uint32_t h,
   j.quality = quality;
   j.format = format;
   int rc = encode_one(c, &j, nullptr);
-  return finish_output(c, rc, j.out, out, out_len);
+  return finish_output(c, rc, j, out, out_len);
 }
 
 // Quality metrics of the page the last wave encoded (a single-page wave
@@ -1164,7 +1311,7 @@ int jp2g_encode_with_psnr(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h
   j.format = format;
   int rc = encode_one(c, &j, nullptr);
   if (rc == JP2G_OK) rc = page_metrics(c, j, psnr_db, ssim);
-  return finish_output(c, rc, j.out, out, out_len);
+  return finish_output(c, rc, j, out, out_len);
 }
 
 static void job_from_request(const jp2g_request& r, PageJob* j) {
@@ -1192,9 +1339,6 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
     outs[i] = nullptr;
     out_lens[i] = 0;
   }
-  // Host Tier-2 of wave k runs on its own thread while wave k+1 is on the
-  // device.
-  std::thread host;
   int rc = JP2G_OK;
   uint64_t counters[8] = {};
   std::memset(c->stage_ms, 0, sizeof c->stage_ms);
@@ -1226,13 +1370,7 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
     for (int k = 0; k < 8; ++k) counters[k] += c->counters[k];
     if (rc != JP2G_OK) break;
     add_wave_stage_times(c);
-    if (host.joinable()) host.join();
-    const int threads = host_threads(c);
-    host = std::thread([wave, threads] {
-      parallel_for(wave.size(), threads, [&](size_t i) { finish_page(wave[i]); });
-    });
   }
-  if (host.joinable()) host.join();
   std::memcpy(c->counters, counters, sizeof counters);
   if (c->timing) {
     // batch: device stages summed over waves; host = wall time not covered
@@ -1248,16 +1386,13 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
   int first_fail = JP2G_OK;
   for (uint32_t i = 0; i < n; ++i) {
     status[i] = jobs[i].status;
-    if (jobs[i].status == JP2G_OK) {
-      std::vector<uint8_t>& b = jobs[i].out;
-      uint8_t* p = static_cast<uint8_t*>(std::malloc(std::max<size_t>(b.size(), 1)));
-      if (!p) {
-        status[i] = JP2G_ENCODE_FAILED;
-      } else {
-        std::memcpy(p, b.data(), b.size());
-        outs[i] = p;
-        out_lens[i] = b.size();
-      }
+    if (jobs[i].status == JP2G_OK && jobs[i].cs) {
+      outs[i] = jobs[i].cs;
+      out_lens[i] = jobs[i].cs_len;
+      jobs[i].cs = nullptr;
+      jobs[i].cs_len = 0;
+    } else if (jobs[i].status == JP2G_OK) {
+      status[i] = JP2G_ENCODE_FAILED;
     } else if (first_fail == JP2G_OK) {
       first_fail = jobs[i].status;
       set_msg(c, "page " + std::to_string(i) + ": " + jobs[i].err);
@@ -1314,10 +1449,10 @@ void worker_loop(jp2g_ctx* c) {
   }
 }
 
-// Finisher: Tier-2 of each finished wave's pages on the host threads, then
-// marks their tickets done (a cancelled ticket's result is dropped). It
-// exits once stopping, with nothing queued, no wave on the device (inflight)
-// and nothing left to finish.
+// Finisher: marks the tickets of each finished wave done (a cancelled
+// ticket's result is dropped) while the worker already runs the next wave.
+// It exits once stopping, with nothing queued, no wave on the device
+// (inflight) and nothing left to finish.
 void finisher_loop(jp2g_ctx* c) {
   for (;;) {
     std::vector<std::shared_ptr<Ticket>> wave;
@@ -1330,9 +1465,6 @@ void finisher_loop(jp2g_ctx* c) {
       wave = std::move(c->finishing.front());
       c->finishing.pop_front();
     }
-    parallel_for(wave.size(), host_threads(c), [&](size_t i) {
-      if (!wave[i]->cancelled) finish_page(&wave[i]->job);
-    });
     {
       std::lock_guard<std::mutex> lk(c->qmu);
       for (auto& t : wave) {
@@ -1340,8 +1472,7 @@ void finisher_loop(jp2g_ctx* c) {
         if (t->cancelled) {
           t->job.status = kEncodeFailed;
           t->job.err = "request cancelled";
-          t->job.out.clear();
-          t->job.out.shrink_to_fit();
+          t->job.drop_output();
         }
       }
     }
@@ -1395,7 +1526,7 @@ int jp2g_poll(jp2g_ctx* c, uint64_t ticket, uint8_t** out, size_t* out_len, int 
   // the result is the ticket's own; the engine mutex (held by the worker
   // for the whole device phase of a wave) is not needed
   if (t->job.status != JP2G_OK) return set_err(c, t->job.status, t->job.err);
-  return finish_output(c, JP2G_OK, t->job.out, out, out_len);
+  return finish_output(c, JP2G_OK, t->job, out, out_len);
 }
 
 int jp2g_cancel(jp2g_ctx* c, uint64_t ticket) {
@@ -1583,7 +1714,7 @@ int jp2g_set_timing(jp2g_ctx* c, int enabled) {
 
 int jp2g_stage_times(jp2g_ctx* c, float* ms, int n) {
   if (!c || !ms) return 0;
-  int k = std::min(n, (int)kNumStages + 3);
+  int k = std::min(n, (int)kNumStages + 4);
   for (int i = 0; i < k; ++i) ms[i] = c->stage_ms[i];
   return k;
 }
@@ -1657,12 +1788,13 @@ int jp2g_debug_blocks(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, ui
   j.ncomp = ncomp;
   j.quality = quality;
   std::vector<BlockOut> res;
+  std::vector<BlockKeep> keep;
   WaveDebug dbg;
   dbg.res = &res;
+  dbg.keep = &keep;
   int rc = encode_one(c, &j, &dbg);
   if (rc) return rc;
   const PagePlan& p = j.plan;
-  const std::vector<BlockKeep>& keep = j.keep;
   *nblocks = p.nblocks;
   for (uint32_t i = 0; i < p.nblocks && i < cap && rows; ++i) {
     int32_t* r = rows + 8 * i;
@@ -1676,6 +1808,46 @@ int jp2g_debug_blocks(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h, ui
     r[7] = (int32_t)keep[i].body_len;
   }
   return JP2G_OK;
+}
+
+int jp2g_debug_assemble_device(jp2g_ctx* c, uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int format,
+                               const uint16_t* npasses, const uint8_t* zbp, const uint32_t* seg_len,
+                               const uint8_t* body, uint32_t nblocks, uint8_t** out, size_t* out_len) {
+  if (!c) return JP2G_INVALID_INPUT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!out || !out_len || (nblocks > 0 && (!npasses || !zbp || !seg_len)))
+    return set_err(c, JP2G_INVALID_INPUT, "null pointer");
+  cudaSetDevice(c->device);
+  PageJob j;
+  Failure f{};
+  if (!build_plan(w, h, (int)ncomp, quality, format, &j.plan, &f)) return set_err(c, f.code, f.msg);
+  if (nblocks != j.plan.nblocks) return set_err(c, JP2G_INVALID_INPUT, "block count does not match the plan");
+  std::vector<BlockKeep> keep(std::max<uint32_t>(nblocks, 1));
+  std::vector<uint32_t> offsets((size_t)nblocks + 1, 0);
+  for (uint32_t i = 0; i < nblocks; ++i) {
+    BlockKeep k{};
+    k.npasses = npasses[i];
+    k.zbp = zbp[i];
+    k.seg_len = npasses[i] ? seg_len[i] : 0;
+    k.body_len = k.seg_len;
+    keep[i] = k;
+    offsets[i + 1] = offsets[i] + k.body_len;
+  }
+  const uint32_t total = offsets[nblocks];
+  if (total > 0 && !body) return set_err(c, JP2G_INVALID_INPUT, "null body");
+  if (!reserve(c, c->keep, keep.size() * sizeof(BlockKeep)) || !reserve(c, c->offsets, offsets.size() * 4) ||
+      !reserve(c, c->body, std::max<uint32_t>(total, 1)) ||
+      !cuda_ok(c, cudaMemcpyAsync(c->keep.p, keep.data(), keep.size() * sizeof(BlockKeep), cudaMemcpyHostToDevice,
+                                  c->stream), "H2D keep") ||
+      !cuda_ok(c, cudaMemcpyAsync(c->offsets.p, offsets.data(), offsets.size() * 4, cudaMemcpyHostToDevice, c->stream),
+               "H2D offsets") ||
+      (total > 0 && !cuda_ok(c, cudaMemcpyAsync(c->body.p, body, total, cudaMemcpyHostToDevice, c->stream), "H2D body")))
+    return JP2G_ENCODE_FAILED;
+  std::vector<PageJob*> live{&j};
+  if (int rc = run_tier2(c, live, dptr<BlockKeep>(c->keep), dptr<uint32_t>(c->offsets), dptr<uint8_t>(c->body), total))
+    return rc;
+  if (j.status != kOk) return set_err(c, j.status, j.err);
+  return finish_output(c, JP2G_OK, j, out, out_len);
 }
 
 int jp2g_debug_assemble(uint32_t w, uint32_t h, uint32_t ncomp, uint8_t quality, int format,

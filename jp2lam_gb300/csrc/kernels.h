@@ -115,6 +115,52 @@ struct PcrdArgs {
 
 void launch_pcrd(const PcrdArgs& a, cudaStream_t st);
 
+// ------------------------------------------------------ device Tier-2 --
+struct T2Node {  // tag-tree node: minimum zero bit-planes, first included leaf (or ~0)
+  uint32_t zmin;
+  uint32_t first_inc;
+};
+struct T2Band {
+  uint32_t first_block;  // in the wave's work list
+  uint32_t tree_off;     // its tag-tree nodes in T2Args::tree
+  uint16_t ncbx, ncby;
+};
+struct T2Packet {  // the bands of one (resolution, component) of a page
+  uint32_t band0, nbands;
+  uint32_t raw_off;  // its unstuffed header bits (words of T2Args::raw)
+  uint32_t hdr_off;  // its header bytes (T2Args::hdr)
+  uint32_t b0, b1;   // its code-blocks [b0, b1) in the wave's work list
+  uint32_t page;
+  uint32_t pad;
+};
+struct T2Page {
+  uint32_t packet0, npackets;
+  uint32_t tmpl_off, tmpl_len;  // the marker prefix (JP2 boxes, SOC..SOD) in T2Args::tmpl
+  uint32_t psot_pos, jp2c_pos;  // fields filled in once the payload is known (jp2c: ~0 for J2K)
+};
+struct T2Args {
+  const T2Packet* packets;
+  uint32_t npackets;
+  const T2Band* bands;
+  const T2Page* pages;
+  uint32_t npages;
+  const BlockKeep* keep;
+  const uint32_t* offsets;  // retained bytes of each block in `body` (nblocks + 1)
+  const uint8_t* body;
+  const uint8_t* tmpl;
+  T2Node* tree;
+  uint32_t* raw;  // zeroed before the launch
+  uint8_t* hdr;
+  uint32_t* hdr_len;   // per packet
+  uint32_t* pkt_off;   // per packet: its offset in its page
+  uint32_t* page_len;  // per page
+  uint32_t* page_off;  // per page (npages + 1): its offset in `out`
+  uint8_t* out;
+};
+// Packet headers, page layout (page_off[npages] = total bytes) and the
+// finished codestreams in `out`. scan_scratch: ceil(npages/1024)+1 words.
+void launch_t2(const T2Args& a, uint32_t* scan_scratch, cudaStream_t st);
+
 // Where a code-block's samples sit in its component's plane (Mallat
 // layout), and its quantiser step.
 struct ReconBlock {

@@ -174,36 +174,14 @@ static void packet_header(const PagePlan& p, size_t band_begin, size_t band_end,
   bw.finish();
 }
 
-bool assemble_codestream(const PagePlan& p, const BlockKeep* keep, const uint8_t* body,
-                         const uint32_t* offsets, std::vector<uint8_t>* out, Failure* err) {
-  // Packet headers first (small), so every length is known before the
-  // output is laid out; then each byte of the output is written once.
-  std::vector<uint8_t> hdr;
-  hdr.reserve(64 * (size_t)(p.levels + 1) * p.ncomp + 1024);
-  struct Packet {
-    size_t hdr_end;       // end of the packet's header in hdr
-    uint32_t body0, body1;  // its body bytes in `body`
-  };
-  std::vector<Packet> packets;
-  uint64_t pay = 0;
-  // bands are stored res -> comp -> orient, i.e. already in packet order
-  size_t bi = 0;
-  while (bi < p.bands.size()) {
-    size_t be = bi;
-    while (be < p.bands.size() && p.bands[be].res == p.bands[bi].res &&
-           p.bands[be].comp == p.bands[bi].comp)
-      ++be;
-    packet_header(p, bi, be, keep, &hdr);
-    const uint32_t b0 = p.bands[bi].first_block;
-    const BandGeom& last = p.bands[be - 1];
-    const uint32_t b1 = last.first_block + (uint32_t)(last.ncbx * last.ncby);
-    packets.push_back({hdr.size(), offsets[b0], offsets[b1]});
-    pay += offsets[b1] - offsets[b0];
-    bi = be;
-  }
-  pay += hdr.size();
-
-  // main header, SOT and SOD
+// The bytes of a page's codestream ahead of its packets: the JP2 boxes (for
+// JP2 output, src/jp2.rs:13-71), SOC, SIZ, COD, QCD, the SOT segment and SOD
+// (src/j2k/markers.rs:8-110, src/j2k/write.rs:9-77), for a packet payload of
+// `payload` bytes. *psot_pos is the offset of the Psot field and *jp2c_pos
+// that of the jp2c box header (~0 for J2K), so a writer that learns the
+// payload later can fill them in. False (with *err) when a length overflows.
+bool codestream_prefix(const PagePlan& p, uint64_t payload, std::vector<uint8_t>* out, uint32_t* psot_pos,
+                       uint32_t* jp2c_pos, Failure* err) {
   std::vector<uint8_t> mh;
   mh.reserve(256);
   be16(mh, 0xff4f);  // SOC
@@ -245,7 +223,7 @@ bool assemble_codestream(const PagePlan& p, const BlockKeep* keep, const uint8_t
     mh.push_back((uint8_t)((p.guard_bits << 5) | 2));
     for (const auto& q : p.quants) be16(mh, (((uint32_t)q.exponent & 0xffu) << 11 | ((uint32_t)q.mantissa & 0x7ffu)) & 0xffffu);
   }
-  const uint64_t psot = 12 + 2 + pay;
+  const uint64_t psot = 12 + 2 + payload;
   if (psot > 0xffffffffull) {
     *err = {kEncodeFailed, "tile-part length exceeds Psot range"};
     return false;
@@ -253,52 +231,88 @@ bool assemble_codestream(const PagePlan& p, const BlockKeep* keep, const uint8_t
   be16(mh, 0xff90);  // SOT
   be16(mh, 10);
   be16(mh, 0);
+  const size_t psot_at = mh.size();
   be32(mh, (uint32_t)psot);
   mh.push_back(0);
   mh.push_back(1);
   be16(mh, 0xff93);  // SOD
-  const uint64_t cs_len = mh.size() + pay + 2;  // + EOC
+  const uint64_t cs_len = mh.size() + payload + 2;  // + EOC
 
-  // JP2 boxes ahead of the codestream (src/jp2.rs:13-71)
-  std::vector<uint8_t> boxes;
+  std::vector<uint8_t>& o = *out;
+  o.clear();
+  *jp2c_pos = ~0u;
   if (p.format == 1) {
     const uint64_t jl = cs_len + 8;
     if (jl > 0xffffffffull) {
       *err = {kEncodeFailed, "JP2 box length exceeds 32-bit limit"};
       return false;
     }
-    boxes.reserve(96);
     auto box = [&](uint32_t len, const char* t) {
-      be32(boxes, len);
-      boxes.insert(boxes.end(), t, t + 4);
+      be32(o, len);
+      o.insert(o.end(), t, t + 4);
     };
     box(12, "jP  ");
-    boxes.insert(boxes.end(), {0x0d, 0x0a, 0x87, 0x0a});
+    o.insert(o.end(), {0x0d, 0x0a, 0x87, 0x0a});
     box(20, "ftyp");
-    boxes.insert(boxes.end(), {'j', 'p', '2', ' '});
-    be32(boxes, 0);
-    boxes.insert(boxes.end(), {'j', 'p', '2', ' '});
+    o.insert(o.end(), {'j', 'p', '2', ' '});
+    be32(o, 0);
+    o.insert(o.end(), {'j', 'p', '2', ' '});
     box(8 + 22 + 15, "jp2h");
     box(22, "ihdr");
-    be32(boxes, p.height);
-    be32(boxes, p.width);
-    be16(boxes, p.ncomp);
-    boxes.insert(boxes.end(), {7, 7, 0, 0});  // BPC, compression type 7, UnkC, IPR
+    be32(o, p.height);
+    be32(o, p.width);
+    be16(o, p.ncomp);
+    o.insert(o.end(), {7, 7, 0, 0});  // BPC, compression type 7, UnkC, IPR
     box(15, "colr");
-    boxes.insert(boxes.end(), {1, 0, 0});
-    be32(boxes, p.srgb ? 16 : 17);
+    o.insert(o.end(), {1, 0, 0});
+    be32(o, p.srgb ? 16 : 17);
+    *jp2c_pos = (uint32_t)o.size();
     box((uint32_t)jl, "jp2c");
   }
+  *psot_pos = (uint32_t)(o.size() + psot_at);
+  o.insert(o.end(), mh.begin(), mh.end());
+  return true;
+}
 
+bool assemble_codestream(const PagePlan& p, const BlockKeep* keep, const uint8_t* body,
+                         const uint32_t* offsets, std::vector<uint8_t>* out, Failure* err) {
+  // Packet headers first (small), so every length is known before the
+  // output is laid out; then each byte of the output is written once.
+  std::vector<uint8_t> hdr;
+  hdr.reserve(64 * (size_t)(p.levels + 1) * p.ncomp + 1024);
+  struct Packet {
+    size_t hdr_end;       // end of the packet's header in hdr
+    uint32_t body0, body1;  // its body bytes in `body`
+  };
+  std::vector<Packet> packets;
+  uint64_t pay = 0;
+  // bands are stored res -> comp -> orient, i.e. already in packet order
+  size_t bi = 0;
+  while (bi < p.bands.size()) {
+    size_t be = bi;
+    while (be < p.bands.size() && p.bands[be].res == p.bands[bi].res &&
+           p.bands[be].comp == p.bands[bi].comp)
+      ++be;
+    packet_header(p, bi, be, keep, &hdr);
+    const uint32_t b0 = p.bands[bi].first_block;
+    const BandGeom& last = p.bands[be - 1];
+    const uint32_t b1 = last.first_block + (uint32_t)(last.ncbx * last.ncby);
+    packets.push_back({hdr.size(), offsets[b0], offsets[b1]});
+    pay += offsets[b1] - offsets[b0];
+    bi = be;
+  }
+  pay += hdr.size();
+  std::vector<uint8_t> pre;
+  uint32_t psot_pos, jp2c_pos;
+  if (!codestream_prefix(p, pay, &pre, &psot_pos, &jp2c_pos, err)) return false;
   std::vector<uint8_t>& o = *out;
-  o.resize(boxes.size() + cs_len);
+  o.resize(pre.size() + pay + 2);
   uint8_t* w = o.data();
   auto put = [&](const uint8_t* src, size_t n) {
     if (n) std::memcpy(w, src, n);
     w += n;
   };
-  put(boxes.data(), boxes.size());
-  put(mh.data(), mh.size());
+  put(pre.data(), pre.size());
   size_t h0 = 0;
   for (const Packet& k : packets) {
     put(hdr.data() + h0, k.hdr_end - h0);
