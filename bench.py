@@ -417,11 +417,20 @@ def bench_served(jl, local, args, pool):
         if i == len(rates) - 1 and r["sustained"] and rate < args.serve_max_rate:
             rates.append(rate + 50)  # still keeping up: extend the sweep
         i += 1
-    knee = max((r["offered_pages_per_s"] for r in rows if r["sustained"]), default=None)
-    confirm = None
-    if knee and args.serve_requests > 0:
-        confirm = _serve_run(eng, knee, args.serve_requests, rng, pool, thumbs)
-        confirm["sustained"] = _sustained(confirm)
+    # the highest sustained rate whose long run (args.serve_requests
+    # requests) is sustained too, trying at most three rates downward
+    knee, confirm = None, None
+    tried = []
+    for rate in sorted((r["offered_pages_per_s"] for r in rows if r["sustained"]), reverse=True)[:3]:
+        if args.serve_requests <= 0:
+            knee = rate
+            break
+        run = _serve_run(eng, rate, args.serve_requests, rng, pool, thumbs)
+        run["sustained"] = _sustained(run)
+        tried.append({"offered_pages_per_s": rate, "sustained": run["sustained"], "p99_ms": run["p99_ms"]})
+        if run["sustained"]:
+            knee, confirm = rate, run
+            break
     eng.close()
     return {"workload": "Poisson arrivals (seed 42), 70% pages of the uneven mix (the uneven batch's "
                         f"{len(pool)} pages) / 30% 256x256 gray q60 thumbnails, JP2, 40 GB device "
@@ -431,8 +440,8 @@ def bench_served(jl, local, args, pool):
             "rates": rows, "p99_objective_ms": SERVE_P99_SLO_MS,
             "sustained_rule": "completions >= 98% of arrivals - 3 over the steady window (after its first "
                               "0.5 s, before the last arrival), p99 <= objective, later-half p99 <= "
-                              "1.25 x earlier-half p99 + 50 ms",
-            "highest_sustained_pages_per_s": knee, "at_knee": confirm,
+                              "1.25 x earlier-half p99 + 50 ms; the reported rate's long run meets it too",
+            "highest_sustained_pages_per_s": knee, "at_knee": confirm, "long_runs_tried": tried,
             "plain_pages_per_s": plain_pps}
 
 
@@ -487,9 +496,9 @@ def main():
     ap.add_argument("--batch-pages", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--uneven-pages", type=int, default=256)
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[50, 100, 200, 300, 350, 400])
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[50, 100, 200, 400, 600])
     ap.add_argument("--serve-seconds", type=float, default=4.0)
-    ap.add_argument("--serve-max-rate", type=float, default=800)
+    ap.add_argument("--serve-max-rate", type=float, default=1500)
     ap.add_argument("--serve-requests", type=int, default=10000,
                     help="requests of the confirmation run at the highest sustained rate (0: none)")
     args = ap.parse_args()

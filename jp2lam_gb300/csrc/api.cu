@@ -109,7 +109,7 @@ struct jp2g_ctx {
   DevBuf px, ll0, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
       hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, planes, signs, sym, stats,
       dwtargs, dwtbases, mqorder, mqscratch, recon, reconblk, t2pk, t2bd, t2pg, t2tmpl, t2tree, t2raw, t2hdr,
-      t2hdrlen, t2pktoff, t2pagelen, t2pageoff, t2out;
+      t2hdrlen, t2pktoff, t2pagelen, t2pageoff, t2nchunks, t2chunkbase, t2out;
   // pinned host staging
   HostBuf hpx, hpx2, hkeep, hres, hcount, hpageoff, hout;
   bool timing = false;
@@ -632,8 +632,9 @@ int run_tier2(jp2g_ctx* c, const std::vector<PageJob*>& live, const BlockKeep* d
       !reserve(c, c->t2tree, std::max<uint64_t>(tree_nodes, 1) * sizeof(T2Node)) ||
       !reserve(c, c->t2raw, (raw_words + 2) * 4) || !reserve(c, c->t2hdr, hdr_bytes) ||
       !reserve(c, c->t2hdrlen, npk * 4) || !reserve(c, c->t2pktoff, npk * 4) || !reserve(c, c->t2pagelen, npg * 4) ||
-      !reserve(c, c->t2pageoff, (npg + 1) * 4) || !reserve(c, c->t2out, out_bound) ||
-      !reserve(c, c->scratch, ((size_t)npg / 1024 + 2) * 4) ||
+      !reserve(c, c->t2pageoff, (npg + 1) * 4) || !reserve(c, c->t2nchunks, npk * 4) ||
+      !reserve(c, c->t2chunkbase, (npk + 1) * 4) || !reserve(c, c->t2out, out_bound) ||
+      !reserve(c, c->scratch, ((size_t)std::max(npg, npk) / 1024 + 2) * 4) ||
       !reserve_host(c, c->hpageoff, (npg + 1) * 4))
     return kEncodeFailed;
   if (!cuda_ok(c, cudaMemcpyAsync(c->t2pk.p, pks.data(), npk * sizeof(T2Packet), cudaMemcpyHostToDevice, c->stream),
@@ -663,9 +664,11 @@ int run_tier2(jp2g_ctx* c, const std::vector<PageJob*>& live, const BlockKeep* d
   a.pkt_off = dptr<uint32_t>(c->t2pktoff);
   a.page_len = dptr<uint32_t>(c->t2pagelen);
   a.page_off = dptr<uint32_t>(c->t2pageoff);
+  a.nchunks = dptr<uint32_t>(c->t2nchunks);
+  a.chunk_base = dptr<uint32_t>(c->t2chunkbase);
   a.out = dptr<uint8_t>(c->t2out);
-  launch_t2(a, dptr<uint32_t>(c->scratch), c->stream);
-  c->counters[5] += 3 + (npg > 1024 ? 1 : 0);
+  launch_t2(a, dptr<uint32_t>(c->scratch), c->num_sms, c->stream);
+  c->counters[5] += 6 + (npg > 1024 ? 1 : 0) + (npk > 1024 ? 1 : 0);
   record(c, kEvT2End);
   const uint32_t* hoff = reinterpret_cast<const uint32_t*>(c->hpageoff.p);
   if (!cuda_ok(c, cudaMemcpyAsync(c->hpageoff.p, a.page_off, (npg + 1) * 4, cudaMemcpyDeviceToHost, c->stream),
@@ -968,7 +971,7 @@ void release_pools(jp2g_ctx* c) {
                     &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
                     &c->mqorder, &c->mqscratch, &c->recon, &c->reconblk, &c->t2pk, &c->t2bd, &c->t2pg,
                     &c->t2tmpl, &c->t2tree, &c->t2raw, &c->t2hdr, &c->t2hdrlen, &c->t2pktoff, &c->t2pagelen,
-                    &c->t2pageoff, &c->t2out};
+                    &c->t2pageoff, &c->t2nchunks, &c->t2chunkbase, &c->t2out};
   for (DevBuf* b : bufs) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -1172,7 +1175,7 @@ void jp2g_destroy(jp2g_ctx* c) {
                     &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
                     &c->mqorder, &c->mqscratch, &c->recon, &c->reconblk, &c->t2pk, &c->t2bd, &c->t2pg,
                     &c->t2tmpl, &c->t2tree, &c->t2raw, &c->t2hdr, &c->t2hdrlen, &c->t2pktoff, &c->t2pagelen,
-                    &c->t2pageoff, &c->t2out};
+                    &c->t2pageoff, &c->t2nchunks, &c->t2chunkbase, &c->t2out};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   HostBuf* hb[] = {&c->hpx, &c->hpx2, &c->hkeep, &c->hres, &c->hcount, &c->hpageoff, &c->hout};

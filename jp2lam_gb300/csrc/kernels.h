@@ -155,11 +155,14 @@ struct T2Args {
   uint32_t* pkt_off;   // per packet: its offset in its page
   uint32_t* page_len;  // per page
   uint32_t* page_off;  // per page (npages + 1): its offset in `out`
+  uint32_t* nchunks;     // per packet: copy jobs
+  uint32_t* chunk_base;  // per packet (npackets + 1): first copy job
   uint8_t* out;
 };
 // Packet headers, page layout (page_off[npages] = total bytes) and the
-// finished codestreams in `out`. scan_scratch: ceil(npages/1024)+1 words.
-void launch_t2(const T2Args& a, uint32_t* scan_scratch, cudaStream_t st);
+// finished codestreams in `out`. scan_scratch: ceil(max(npages,
+// npackets)/1024)+1 words.
+void launch_t2(const T2Args& a, uint32_t* scan_scratch, int num_sms, cudaStream_t st);
 
 // Where a code-block's samples sit in its component's plane (Mallat
 // layout), and its quantiser step.

@@ -5,9 +5,8 @@
 // and the codestream/JP2 writers (src/j2k/write.rs:9-77, src/jp2.rs:13-71)
 // for the device path: only the finished codestreams cross to the host.
 //
-// One warp per packet (one layer, one precinct: a packet is the bands of one
-// (resolution, component)). The bits of a packet header are laid out in
-// parallel:
+// A packet is the bands of one (resolution, component) (one layer, one
+// precinct). The bits of a packet header are laid out in parallel:
 //  - a tag tree's node values are minima over its leaves (level by level);
 //  - with one layer a node's bits are emitted only once, by the first leaf
 //    (in raster order) whose walk reaches it: for the inclusion tree every
@@ -16,14 +15,16 @@
 //    included leaf of the region (ISO/IEC 15444-1 B.10.2);
 //  - so every code-block knows its own header bits (inclusion, zero
 //    bit-planes, Table B-4 pass count, Lblock comma code and length,
-//    B.10.4-B.10.7), a warp prefix sum gives their positions, and each lane
+//    B.10.4-B.10.7), a prefix sum gives their positions, and each thread
 //    ORs its bits into an unstuffed big-endian bitstream;
-//  - a second warp pass cuts the bitstream into bytes, a byte after 0xFF
+//  - a warp pass cuts the bitstream into bytes, a byte after 0xFF
 //    taking only 7 bits (B.10.1), and ends the header with a zero byte when
 //    its last byte is 0xFF.
-// A second kernel places every page: the host-built marker template (JP2
-// boxes, SOC..SOD) with Psot and the jp2c box length filled in, each
-// packet's header and body, EOC.
+// One CTA per packet: the tag trees and, for the stuffing pass, the
+// header's bits are staged in shared memory. The pages are then placed by
+// copy jobs of 16 KiB spread over the whole GPU (each packet's header and
+// body), and one warp per page writes the host-built marker prefix (JP2
+// boxes, SOC..SOD) with Psot and the jp2c box length filled in, and EOC.
 #include <cuda_runtime.h>
 
 #include "jp2g_internal.h"
@@ -123,19 +124,23 @@ __device__ uint32_t leaf_bits(const LevelGeom& g, const T2Node* tree, uint32_t l
   return pos - p0;
 }
 
-__global__ void __launch_bounds__(128) t2_header_kernel(T2Args a) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t pk_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (pk_id >= a.npackets) return;
+constexpr int kT2Threads = 256;
+constexpr int kT2SmemNodes = 4096;     // tag trees of bands up to ~3,000 code-blocks; then the header bits
+constexpr uint32_t kT2Chunk = 16384;   // bytes of output one copy job moves
+
+__global__ void __launch_bounds__(kT2Threads) t2_header_kernel(T2Args a) {
+  __shared__ uint64_t sbuf[kT2SmemNodes];
+  __shared__ uint32_t wsum[kT2Threads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const uint32_t pk_id = blockIdx.x;
   const T2Packet pk = a.packets[pk_id];
   uint32_t* raw = a.raw + pk.raw_off;
   uint32_t pos = 1;  // bit 0: the packet is present (t2.rs:337-344)
-  if (lane == 0) put_bits(raw, 0, 1u, 1);
+  if (tid == 0) put_bits(raw, 0, 1u, 1);
   for (uint32_t bi = pk.band0; bi < pk.band0 + pk.nbands; ++bi) {
     const T2Band bd = a.bands[bi];
     const uint32_t n = (uint32_t)bd.ncbx * bd.ncby;
     if (n == 0) continue;
-    T2Node* tree = a.tree + bd.tree_off;
     LevelGeom g;
     {
       uint32_t w = bd.ncbx, h = bd.ncby, off = 0;
@@ -150,16 +155,19 @@ __global__ void __launch_bounds__(128) t2_header_kernel(T2Args a) {
         h = (h + 1) / 2;
       }
     }
+    // the band's tag trees in shared memory when they fit
+    const uint32_t nodes = g.off[g.n - 1] + 1;
+    T2Node* tree = nodes <= (uint32_t)kT2SmemNodes ? reinterpret_cast<T2Node*>(sbuf) : a.tree + bd.tree_off;
     // leaves, then each level's minima
-    for (uint32_t i = lane; i < n; i += 32) {
+    for (uint32_t i = tid; i < n; i += kT2Threads) {
       const BlockKeep k = a.keep[bd.first_block + i];
       tree[i] = T2Node{k.zbp, k.npasses > 0 ? i : kNone};
     }
-    __syncwarp();
+    __syncthreads();
     for (int l = 1; l < g.n; ++l) {
       const uint32_t cw = g.w[l - 1], ch = (g.off[l] - g.off[l - 1]) / cw, w = g.w[l];
       const uint32_t h = (ch + 1) / 2;
-      for (uint32_t k = lane; k < w * h; k += 32) {
+      for (uint32_t k = tid; k < w * h; k += kT2Threads) {
         const uint32_t x = k % w, y = k / w;
         uint32_t z = 0xffffffffu, f = kNone;
         for (uint32_t dy = 0; dy < 2; ++dy)
@@ -172,11 +180,11 @@ __global__ void __launch_bounds__(128) t2_header_kernel(T2Args a) {
           }
         tree[g.off[l] + k] = T2Node{z, f};
       }
-      __syncwarp();
+      __syncthreads();
     }
-    // header bits of the band's blocks, 32 at a time in raster order
-    for (uint32_t c0 = 0; c0 < n; c0 += 32) {
-      const uint32_t i = c0 + lane;
+    // header bits of the band's blocks, 256 at a time in raster order
+    for (uint32_t c0 = 0; c0 < n; c0 += kT2Threads) {
+      const uint32_t i = c0 + tid;
       uint32_t cnt = 0;
       BlockKeep k{};
       const int x = (int)(i % bd.ncbx), y = (int)(i / bd.ncbx);
@@ -190,15 +198,33 @@ __global__ void __launch_bounds__(128) t2_header_kernel(T2Args a) {
         const uint32_t t = __shfl_up_sync(~0u, incl, o);
         if (lane >= o) incl += t;
       }
-      if (i < n) leaf_bits(g, tree, i, x, y, k, raw, pos + incl - cnt);
-      pos += __shfl_sync(~0u, incl, 31);
+      if (lane == 31) wsum[wid] = incl;
+      __syncthreads();
+      uint32_t before = 0, total = 0;
+      #pragma unroll
+      for (int k2 = 0; k2 < kT2Threads / 32; ++k2) {
+        before += k2 < wid ? wsum[k2] : 0u;
+        total += wsum[k2];
+      }
+      if (i < n) leaf_bits(g, tree, i, x, y, k, raw, pos + before + incl - cnt);
+      pos += total;
+      __syncthreads();
     }
-    __syncwarp();
   }
-  __syncwarp();
+  __syncthreads();  // every bit is in `raw`
+  // stage the bits in shared memory when they fit
+  const uint32_t nbits = pos;
+  const uint32_t nwords = (nbits + 31) / 32 + 2;  // the slot has two words of slack
+  const uint32_t* rb = raw;
+  if (nwords <= 2u * kT2SmemNodes) {
+    uint32_t* s32 = reinterpret_cast<uint32_t*>(sbuf);
+    for (uint32_t wd = tid; wd < nwords; wd += kT2Threads) s32[wd] = raw[wd];
+    __syncthreads();
+    rb = s32;
+  }
+  if (wid != 0) return;
   // bytes: 8 bits each, 7 after a 0xFF byte; a final 0xFF is followed by a
   // zero byte (ISO/IEC 15444-1 B.10.1)
-  const uint32_t nbits = pos;
   uint8_t* out = a.hdr + pk.hdr_off;
   uint32_t p = 0, nout = 0;
   bool prev_ff = false;
@@ -207,7 +233,7 @@ __global__ void __launch_bounds__(128) t2_header_kernel(T2Args a) {
     const uint32_t start = p + (lane == 0 ? 0u : w0 + 8u * (uint32_t)(lane - 1));
     const int width = lane == 0 ? (int)w0 : 8;
     const bool valid = start < nbits;
-    const uint32_t byte = valid ? get_bits(raw, start, width) : 0u;
+    const uint32_t byte = valid ? get_bits(rb, start, width) : 0u;
     const uint32_t ff = __ballot_sync(~0u, valid && byte == 0xffu);
     const uint32_t vm = __ballot_sync(~0u, valid);
     const int last = ff ? __ffs(ff) - 1 : 31;  // bytes after a 0xFF need the 7-bit rule
@@ -224,7 +250,8 @@ __global__ void __launch_bounds__(128) t2_header_kernel(T2Args a) {
   if (lane == 0) a.hdr_len[pk_id] = nout;
 }
 
-// Page layout: every packet's place in its page, and each page's length.
+// Page layout: every packet's place in its page and its number of copy
+// jobs, and each page's length.
 __global__ void t2_layout_kernel(T2Args a) {
   const uint32_t pg = blockIdx.x * blockDim.x + threadIdx.x;
   if (pg >= a.npages) return;
@@ -232,10 +259,36 @@ __global__ void t2_layout_kernel(T2Args a) {
   uint32_t off = p.tmpl_len;
   for (uint32_t k = p.packet0; k < p.packet0 + p.npackets; ++k) {
     const T2Packet pk = a.packets[k];
+    const uint32_t len = a.hdr_len[k] + (a.offsets[pk.b1] - a.offsets[pk.b0]);
     a.pkt_off[k] = off;
-    off += a.hdr_len[k] + (a.offsets[pk.b1] - a.offsets[pk.b0]);
+    a.nchunks[k] = (len + kT2Chunk - 1) / kT2Chunk;
+    off += len;
   }
   a.page_len[pg] = off + 2;  // EOC
+}
+
+// Copy jobs over the whole GPU: job j moves up to kT2Chunk bytes of one
+// packet (its header, then its body) into place.
+__global__ void __launch_bounds__(kT2Threads) t2_copy_kernel(T2Args a) {
+  const uint32_t njobs = a.chunk_base[a.npackets];
+  for (uint32_t job = blockIdx.x; job < njobs; job += gridDim.x) {
+    uint32_t lo = 0, hi = a.npackets;  // packet k with chunk_base[k] <= job < chunk_base[k + 1]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) / 2;
+      if (a.chunk_base[mid] <= job) lo = mid;
+      else hi = mid;
+    }
+    const uint32_t k = lo;
+    const T2Packet pk = a.packets[k];
+    uint8_t* o = a.out + a.page_off[pk.page] + a.pkt_off[k];
+    const uint32_t hl = a.hdr_len[k];
+    const uint8_t* h = a.hdr + pk.hdr_off;
+    const uint8_t* b = a.body + a.offsets[pk.b0] - hl;  // body byte i - hl at b[i]
+    const uint32_t len = hl + (a.offsets[pk.b1] - a.offsets[pk.b0]);
+    const uint32_t from = (job - a.chunk_base[k]) * kT2Chunk, to = min(from + kT2Chunk, len);
+    #pragma unroll 4
+    for (uint32_t i = from + threadIdx.x; i < to; i += kT2Threads) o[i] = i < hl ? h[i] : b[i];
+  }
 }
 
 __device__ __forceinline__ void put_be32(uint8_t* o, uint32_t v) {
@@ -245,24 +298,11 @@ __device__ __forceinline__ void put_be32(uint8_t* o, uint32_t v) {
   o[3] = (uint8_t)v;
 }
 
-// One warp per packet copies its header and body; one more warp per page
-// copies the marker template (with Psot and the jp2c length) and EOC.
-__global__ void __launch_bounds__(128) t2_assemble_kernel(T2Args a) {
+// One warp per page: the marker prefix with Psot and the jp2c length
+// filled in, and EOC.
+__global__ void __launch_bounds__(128) t2_pages_kernel(T2Args a) {
   const int lane = threadIdx.x & 31;
-  const uint32_t id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (id < a.npackets) {
-    const T2Packet pk = a.packets[id];
-    uint8_t* o = a.out + a.page_off[pk.page] + a.pkt_off[id];
-    const uint32_t hl = a.hdr_len[id];
-    const uint8_t* h = a.hdr + pk.hdr_off;
-    for (uint32_t i = lane; i < hl; i += 32) o[i] = h[i];
-    o += hl;
-    const uint8_t* b = a.body + a.offsets[pk.b0];
-    const uint32_t bl = a.offsets[pk.b1] - a.offsets[pk.b0];
-    for (uint32_t i = lane; i < bl; i += 32) o[i] = b[i];
-    return;
-  }
-  const uint32_t pg = id - a.npackets;
+  const uint32_t pg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (pg >= a.npages) return;
   const T2Page p = a.pages[pg];
   uint8_t* o = a.out + a.page_off[pg];
@@ -280,12 +320,14 @@ __global__ void __launch_bounds__(128) t2_assemble_kernel(T2Args a) {
 
 }  // namespace
 
-void launch_t2(const T2Args& a, uint32_t* scan_scratch, cudaStream_t st) {
+void launch_t2(const T2Args& a, uint32_t* scan_scratch, int num_sms, cudaStream_t st) {
   if (a.npackets == 0) return;
-  t2_header_kernel<<<(a.npackets + 3) / 4, 128, 0, st>>>(a);
+  t2_header_kernel<<<a.npackets, kT2Threads, 0, st>>>(a);
   t2_layout_kernel<<<(a.npages + 127) / 128, 128, 0, st>>>(a);
   launch_scan_u32(a.page_len, 1, a.npages, a.page_off, scan_scratch, st);
-  t2_assemble_kernel<<<(a.npackets + a.npages + 3) / 4, 128, 0, st>>>(a);
+  launch_scan_u32(a.nchunks, 1, a.npackets, a.chunk_base, scan_scratch, st);
+  t2_copy_kernel<<<(unsigned)num_sms * 8, kT2Threads, 0, st>>>(a);
+  t2_pages_kernel<<<(a.npages + 3) / 4, 128, 0, st>>>(a);
 }
 
 }  // namespace jp2g
