@@ -6,7 +6,7 @@ Run in a container where the reference tree is mounted; it writes
 tests can check the oracle's (and the CUDA path's) tables without the
 reference present.
 
-    python tests/golden/reference_tables.py /root/reference
+    python tests/golden/reference_tables.py <path of the jp2lam source tree>
 """
 import hashlib
 import json
@@ -73,4 +73,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: reference_tables.py <path of the jp2lam source tree>")
+    main(sys.argv[1])
