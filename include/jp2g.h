@@ -72,6 +72,22 @@ int jp2g_encode_with_psnr(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t
                           int interleaved, uint8_t quality, int format, uint8_t** out, size_t* out_len,
                           double* psnr_db, double* ssim);
 
+/* Decodes a J2K or JP2 file as decode_jp2 does (src/decode/mod.rs:56-61):
+ * single tile, one quality layer, LRCP, one precinct per resolution, 8-bit
+ * gray or 3-component, 64x64 or smaller code-blocks — the codestreams this
+ * library and the reference write. The host parses the boxes, the main
+ * header and the packet headers; code-block decoding (MQ decoder and the
+ * three passes), dequantisation, the inverse DWT and inverse RCT/ICT run on
+ * the device. *px (free with jp2g_free) receives w * h * ncomp interleaved
+ * samples. Malformed input gives JP2G_DECODE_FAILED, codestreams outside
+ * that profile JP2G_UNSUPPORTED_FEATURE, each with a message.
+ * flags: JP2G_DECODE_RCT_CHROMA_EXTRA_BITPLANE counts one more magnitude
+ * bit-plane for the chroma of reversible RCT codestreams (the encoder codes
+ * them with it at quality 100, and QCD does not signal it). */
+enum { JP2G_DECODE_RCT_CHROMA_EXTRA_BITPLANE = 1 };
+int jp2g_decode(jp2g_ctx* ctx, const uint8_t* bytes, size_t n, int flags, uint8_t** px, size_t* px_len,
+                uint32_t* w, uint32_t* h, uint32_t* ncomp);
+
 /* Same as jp2g_encode, but `d_px` is interleaved pixel data already resident
  * in device memory (w * h * ncomp bytes). Used for device-resident batching;
  * the reference has no equivalent entry point (its input is always host

@@ -10,6 +10,7 @@ backed by the C ABI in include/jp2g.h (libjp2g.so, CUDA for sm_103a):
     encode_with_psnr(image, options)                (src/encode/mod.rs:115-135)
     BatchEncoder(options).encode_one / encode_all   (src/batch.rs:26-85)
     encode_batch(images, options)                   (src/batch.rs:173-178)
+    decode_jp2(bytes) -> Image                      (src/decode/mod.rs:56-61)
 
 Errors are Jp2LamError subclasses carrying the reference's variant names.
 The compute path is the CUDA library only; if it cannot be loaded or no GPU
@@ -27,7 +28,7 @@ from ._native import Engine, Jp2LamError, InvalidInput, EncodeFailed, DecodeFail
 __all__ = [
     "ColorSpace", "OutputFormat", "Preset", "Image", "Component", "EncodeOptions",
     "encode", "encode_to_writer", "encode_with_psnr", "EncodeMetrics", "BatchEncoder", "BatchProfile", "encode_batch",
-    "encode_pages", "Server", "Engine", "Jp2LamError", "InvalidInput", "EncodeFailed", "DecodeFailed",
+    "encode_pages", "decode_jp2", "Server", "Engine", "Jp2LamError", "InvalidInput", "EncodeFailed", "DecodeFailed",
     "UnsupportedFeature", "IoError",
 ]
 
@@ -167,6 +168,19 @@ def encode_with_psnr(image: Image, options: EncodeOptions,
     data, psnr, ssim = eng.encode_with_psnr(image.data, image.width, image.height, image.ncomp,
                                             int(options.quality), int(options.format))
     return data, EncodeMetrics(psnr, ssim)
+
+
+def decode_jp2(data: bytes, engine: Optional[Engine] = None,
+               rct_chroma_extra_bitplane: bool = False) -> Image:
+    """Decode a J2K/JP2 file of this encoder's profile on the GPU
+    (decode_jp2, src/decode/mod.rs:56-61). rct_chroma_extra_bitplane counts
+    the extra chroma bit-plane that lossless sRGB encodes use and QCD does not
+    signal; without it such files can fail as they do in the reference."""
+    eng = engine or default_engine()
+    px, w, h, c = eng.decode(data, rct_chroma_extra_bitplane)
+    if c == 1:
+        return Image.from_gray_bytes(w, h, px)
+    return Image.from_rgb_bytes(w, h, px)
 
 
 @dataclass(frozen=True)

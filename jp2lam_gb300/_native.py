@@ -52,7 +52,7 @@ EXPORTS = [
     "jp2g_debug_coefficients", "jp2g_debug_blocks", "jp2g_dwt_noalloc", "jp2g_tables",
     "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
     "jp2g_autotune", "jp2g_debug_assemble", "jp2g_debug_plan", "jp2g_cancel", "jp2g_debug_context_labels",
-    "jp2g_debug_coefficients_f32", "jp2g_encode_with_psnr", "jp2g_debug_assemble_device",
+    "jp2g_debug_coefficients_f32", "jp2g_encode_with_psnr", "jp2g_debug_assemble_device", "jp2g_decode",
 ]
 
 PENDING = 6
@@ -110,6 +110,10 @@ def load_library(path: str = LIB_PATH):
                                               ctypes.c_uint32, ctypes.c_int, ctypes.c_uint8, ctypes.c_int,
                                               ctypes.POINTER(_u8p), ctypes.POINTER(ctypes.c_size_t),
                                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        lib.jp2g_decode.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                    ctypes.POINTER(_u8p), ctypes.POINTER(ctypes.c_size_t),
+                                    ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                                    ctypes.POINTER(ctypes.c_uint32)]
         lib.jp2g_debug_blocks.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8,
                                           ctypes.c_void_p, ctypes.c_uint32,
@@ -209,6 +213,22 @@ class Engine:
         data = ctypes.string_at(out, n.value)
         self.lib.jp2g_free(out)
         return data, psnr.value, ssim.value
+
+    def decode(self, data: bytes, rct_chroma_extra_bitplane: bool = False):
+        """(pixels, w, h, ncomp): a J2K/JP2 file decoded on the device
+        (decode_jp2, src/decode/mod.rs:56-61); pixels interleaved."""
+        buf = np.frombuffer(bytes(data), dtype=np.uint8)
+        out = _u8p()
+        n = ctypes.c_size_t()
+        w, h, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        with self._lock:
+            rc = self.lib.jp2g_decode(self.handle, buf.ctypes.data_as(ctypes.c_void_p), buf.size,
+                                      1 if rct_chroma_extra_bitplane else 0, ctypes.byref(out), ctypes.byref(n),
+                                      ctypes.byref(w), ctypes.byref(h), ctypes.byref(c))
+            self._check(rc)
+        px = ctypes.string_at(out, n.value)
+        self.lib.jp2g_free(out)
+        return px, w.value, h.value, c.value
 
     def encode_device(self, dev_ptr: int, w: int, h: int, ncomp: int, quality: int, fmt: int) -> bytes:
         out = _u8p()

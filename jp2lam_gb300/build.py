@@ -19,7 +19,8 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libjp2g.so")
 SYNTH_LIB = os.path.join(OUT_DIR, "libjp2g_synth.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["api.cu", "dwt.cu", "t1.cu", "pcrd.cu", "recon.cu", "t2dev.cu", "plan.cpp", "t2.cpp", "tables.cpp", "noalloc.cu"]
+SOURCES = ["api.cu", "dwt.cu", "t1.cu", "pcrd.cu", "recon.cu", "t2dev.cu", "plan.cpp", "t2.cpp", "tables.cpp", "noalloc.cu",
+           "decode.cpp", "t1dec.cu"]
 
 
 def nvcc():

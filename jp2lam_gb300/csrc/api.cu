@@ -1317,6 +1317,65 @@ int jp2g_encode_with_psnr(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h
   return finish_output(c, rc, j, out, out_len);
 }
 
+// decode_jp2 (src/decode/mod.rs:56-61) on the device: the host parses the
+// boxes, headers and packet headers (decode.cpp); the code-blocks are decoded
+// and the image reconstructed by kernels (t1dec.cu, recon.cu).
+int jp2g_decode(jp2g_ctx* c, const uint8_t* bytes, size_t n, int flags, uint8_t** px, size_t* px_len, uint32_t* w,
+                uint32_t* h, uint32_t* ncomp) {
+  if (!c) return JP2G_INVALID_INPUT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!px || !px_len || !w || !h || !ncomp) return set_err(c, JP2G_INVALID_INPUT, "output pointer is null");
+  if (!bytes && n) return set_err(c, JP2G_INVALID_INPUT, "input pointer is null");
+  cudaSetDevice(c->device);
+  DecodeLayout L;
+  Failure f{};
+  if (!parse_codestream(bytes, n, (flags & JP2G_DECODE_RCT_CHROMA_EXTRA_BITPLANE) != 0, &L, &f))
+    return set_err(c, f.code, f.msg);
+  const uint64_t npx = (uint64_t)L.width * L.height;
+  if (npx > (1ull << 30)) return set_err(c, JP2G_UNSUPPORTED_FEATURE, "image too large to decode");
+  const size_t plane_bytes = (size_t)npx * L.ncomp * 4, out_bytes = (size_t)npx * L.ncomp;
+  const size_t nb = L.blocks.size();
+  if (!reserve(c, c->t2out, std::max<size_t>(n, 16)) ||
+      !reserve(c, c->reconblk, std::max<size_t>(nb, 1) * sizeof(DecBlock)) ||
+      !reserve(c, c->recon, plane_bytes + (size_t)npx * 4 + out_bytes + 256))
+    return JP2G_DECODE_FAILED;
+  DecodeArgs a{};
+  a.data = dptr<uint8_t>(c->t2out);
+  a.blocks = dptr<DecBlock>(c->reconblk);
+  a.nblocks = (uint32_t)nb;
+  a.width = L.width;
+  a.height = L.height;
+  a.ncomp = L.ncomp;
+  a.reversible = L.reversible;
+  a.mct = L.mct;
+  a.plane = dptr<int32_t>(c->recon);
+  a.tmp = a.plane + npx * L.ncomp;
+  a.px = reinterpret_cast<uint8_t*>(a.tmp + npx);
+  uint8_t* out = static_cast<uint8_t*>(std::malloc(std::max<size_t>(out_bytes, 1)));
+  if (!out) return set_err(c, JP2G_DECODE_FAILED, "out of host memory");
+  if (!cuda_ok(c, cudaMemcpyAsync(c->t2out.p, bytes, n, cudaMemcpyHostToDevice, c->stream), "H2D codestream") ||
+      !cuda_ok(c, cudaMemcpyAsync(c->reconblk.p, L.blocks.data(), nb * sizeof(DecBlock), cudaMemcpyHostToDevice,
+                                  c->stream), "H2D code-blocks") ||
+      !cuda_ok(c, cudaMemsetAsync(a.plane, 0, plane_bytes, c->stream), "memset planes")) {
+    std::free(out);
+    return JP2G_DECODE_FAILED;
+  }
+  launch_t1_decode(a, c->stream);
+  launch_decode_reconstruct(a, L.ladder.data(), L.levels, c->stream);
+  if (!cuda_ok(c, cudaGetLastError(), "decode kernels") ||
+      !cuda_ok(c, cudaMemcpyAsync(out, a.px, out_bytes, cudaMemcpyDeviceToHost, c->stream), "D2H samples") ||
+      !cuda_ok(c, cudaStreamSynchronize(c->stream), "decode")) {
+    std::free(out);
+    return JP2G_DECODE_FAILED;
+  }
+  *px = out;
+  *px_len = out_bytes;
+  *w = L.width;
+  *h = L.height;
+  *ncomp = (uint32_t)L.ncomp;
+  return JP2G_OK;
+}
+
 static void job_from_request(const jp2g_request& r, PageJob* j) {
   (r.on_device ? j->dev_px : j->host_px) = r.px;
   j->w = r.width;

@@ -75,6 +75,7 @@ struct PagePlan {
 
 bool build_plan(uint32_t w, uint32_t h, int ncomp, int quality, int format,
                 PagePlan* plan, Failure* err);
+float quant_step_from_qcd(int precision, int orient, int exponent, int mantissa);
 
 // -------------------------------------------------------- device layout ----
 // Per-block descriptor in the flat work list.

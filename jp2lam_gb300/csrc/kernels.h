@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <utility>
+#include <vector>
 
 #include "jp2g_internal.h"
 
@@ -163,6 +164,46 @@ struct T2Args {
 // finished codestreams in `out`. scan_scratch: ceil(max(npages,
 // npackets)/1024)+1 words.
 void launch_t2(const T2Args& a, uint32_t* scan_scratch, int num_sms, cudaStream_t st);
+
+// ------------------------------------------------------------- decoding --
+// One code-block of a codestream being decoded.
+struct DecBlock {
+  uint32_t data_off, data_len;  // its segment in the input bytes
+  uint32_t x0, y0;              // its samples in its component's plane (Mallat layout)
+  uint16_t w, h;
+  uint8_t comp, orient, mb, zbp;  // mb: bit-planes from QCD (decode/t1.rs:56)
+  uint16_t npasses;
+  uint16_t pad;
+  float step;  // quantiser step (irreversible codestreams)
+};
+
+// What the host parse learns from a codestream (decode.cpp).
+struct DecodeLayout {
+  uint32_t width = 0, height = 0;
+  int ncomp = 0, precision = 0, levels = 0, cbw = 64, cbh = 64, guard = 2;
+  bool reversible = true, mct = false;
+  std::vector<std::pair<int, int>> ladder;  // resolution sizes, index 0 = the smallest
+  std::vector<DecBlock> blocks;
+};
+bool parse_codestream(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane, DecodeLayout* out,
+                      Failure* err);
+
+struct DecodeArgs {
+  const uint8_t* data;  // the input bytes on the device
+  const DecBlock* blocks;
+  uint32_t nblocks;
+  uint32_t width, height;
+  int ncomp, reversible, mct;
+  int32_t* plane;  // ncomp planes of width * height: int32 coefficients, or f32 values when irreversible
+  int32_t* tmp;    // one plane of scratch
+  uint8_t* px;     // width * height * ncomp interleaved output samples
+};
+// Tier-1 decoding of every code-block (t1dec.cu), then dequantisation,
+// the inverse DWT per component, inverse RCT/ICT and the 8-bit samples
+// (recon.cu). plane must be zeroed before.
+void launch_t1_decode(const DecodeArgs& a, cudaStream_t st);
+void launch_decode_reconstruct(const DecodeArgs& a, const std::pair<int, int>* ladder, int levels, cudaStream_t st);
+bool upload_decode_tables(const uint8_t* zc, const uint8_t* sc, const uint8_t* spb, const uint32_t* mq);
 
 // Where a code-block's samples sit in its component's plane (Mallat
 // layout), and its quantiser step.

@@ -24,6 +24,15 @@ double norm97(int level, int orient) {
 
 int band_gain(int orient) { return orient == LL ? 0 : (orient == HH ? 2 : 1); }
 
+// The f32 quantiser step of a band from its QCD exponent and mantissa,
+// floored at 1e-6 (backend.rs:602-620).
+float quant_step_from_qcd(int precision, int orient, int exponent, int mantissa) {
+  const int numbps = precision + band_gain(orient);
+  const float base = 1.0f + (float)mantissa / 2048.0f;
+  const float s = base * std::ldexp(1.0f, numbps - exponent);
+  return s > 1e-6f ? s : 1e-6f;
+}
+
 static int ilog2(int v) { return 31 - __builtin_clz((unsigned)std::max(v, 1)); }
 
 // Step packing: exponent/mantissa of an 8192-scaled step (norms.rs:85-92).
@@ -128,9 +137,7 @@ bool build_plan(uint32_t w, uint32_t h, int ncomp, int quality, int format,
   }
   for (auto& q : p->quants) {
     int numbps = p->precision + band_gain(q.orient);
-    float base = 1.0f + (float)q.mantissa / 2048.0f;
-    float s = base * std::ldexp(1.0f, numbps - q.exponent);
-    q.step_f32 = s > 1e-6f ? s : 1e-6f;
+    q.step_f32 = quant_step_from_qcd(p->precision, q.orient, q.exponent, q.mantissa);
     q.step_f64 = (1.0 + q.mantissa / 2048.0) * std::ldexp(1.0, numbps - q.exponent);
   }
   // Resolution ladder and subband rectangles (layout.rs:37-173).

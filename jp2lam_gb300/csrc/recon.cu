@@ -199,7 +199,109 @@ __global__ void recon_ssim_kernel(ReconArgs r) {
   if (threadIdx.x == 0) atomicAdd(&r.stats[1], s);
 }
 
+// ------------------------------------------------------------- decoding --
+// Reconstruction of a decoded codestream (reconstruct, src/decode/
+// reconstruct.rs:24-304): the inverse 5/3 (src/dwt/rev53.rs:96-129 and
+// 419-497: per level rows then columns; even samples first,
+// s[i] - ((d[i-1] + d[i] + 2) >> 2) with the edges clamped, then odd samples
+// d[i] + ((e[i] + e[i+1]) >> 1), or d[i] + e[i] at the right edge) and
+// inverse RCT, or the inverse 9/7 above and inverse ICT; the level shift and
+// the 8-bit clamp (finalize, src/simd/scalar.rs:216-242).
+
+// Inverse 1-D 5/3 of row y: a warp per row, through the row's slice of tmp.
+__global__ void dec53_rows_kernel(int32_t* plane, int32_t* tmp, int stride, int rw, int rh) {
+  const int lane = threadIdx.x & 31;
+  const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (y >= rh || rw <= 1) return;
+  int32_t* x = plane + (size_t)y * stride;
+  int32_t* t = tmp + (size_t)y * stride;
+  const int sn = (rw + 1) / 2, dn = rw - sn;
+  for (int i = lane; i < sn; i += 32) {
+    const int l = min(max(i - 1, 0), dn - 1), r = min(i, dn - 1);
+    t[2 * i] = x[i] - ((x[sn + l] + x[sn + r] + 2) >> 2);
+  }
+  __syncwarp();
+  for (int i = lane; i < dn; i += 32)
+    t[2 * i + 1] = i + 1 < sn ? x[sn + i] + ((t[2 * i] + t[2 * i + 2]) >> 1) : x[sn + i] + t[2 * i];
+  __syncwarp();
+  for (int i = lane; i < rw; i += 32) x[i] = t[i];
+}
+
+// Inverse 1-D 5/3 of every column x < rw: a thread per column.
+__global__ void dec53_cols_kernel(int32_t* plane, int32_t* tmp, int stride, int rw, int rh) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= rw || rh <= 1) return;
+  int32_t* p = plane + x;
+  int32_t* t = tmp + x;
+  const size_t s = (size_t)stride;
+  const int sn = (rh + 1) / 2, dn = rh - sn;
+  for (int i = 0; i < sn; ++i) {
+    const int l = min(max(i - 1, 0), dn - 1), r = min(i, dn - 1);
+    t[2 * i * s] = p[i * s] - ((p[(sn + l) * s] + p[(sn + r) * s] + 2) >> 2);
+  }
+  for (int i = 0; i < dn; ++i)
+    t[(2 * i + 1) * s] =
+        i + 1 < sn ? p[(sn + i) * s] + ((t[2 * i * s] + t[(2 * i + 2) * s]) >> 1) : p[(sn + i) * s] + t[2 * i * s];
+  for (int i = 0; i < rh; ++i) p[i * s] = t[i * s];
+}
+
+__device__ __forceinline__ uint8_t clamp_int(int32_t v) { return (uint8_t)min(max(v + 128, 0), 255); }
+__device__ __forceinline__ uint8_t clamp_round(float v) {
+  return (uint8_t)(int)fminf(fmaxf(roundf(__fadd_rn(v, 128.0f)), 0.0f), 255.0f);
+}
+
+// Inverse RCT (src/simd/scalar.rs:216-228) or ICT (scalar.rs:201-214) and
+// the interleaved 8-bit samples.
+__global__ void dec_pixels_kernel(DecodeArgs a) {
+  const size_t n = (size_t)a.width * a.height;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (a.reversible) {
+    const int32_t* q = a.plane;
+    if (a.ncomp == 3 && a.mct) {
+      const int32_t yy = q[i], db = q[n + i], dr = q[2 * n + i];
+      const int32_t g = yy - ((db + dr) >> 2);
+      a.px[3 * i] = clamp_int(dr + g);
+      a.px[3 * i + 1] = clamp_int(g);
+      a.px[3 * i + 2] = clamp_int(db + g);
+    } else {
+      for (int c = 0; c < a.ncomp; ++c) a.px[a.ncomp * i + c] = clamp_int(q[c * n + i]);
+    }
+  } else {
+    const float* f = reinterpret_cast<const float*>(a.plane);
+    if (a.ncomp == 3 && a.mct) {
+      const float yy = f[i], cb = f[n + i], cr = f[2 * n + i];
+      a.px[3 * i] = clamp_round(__fadd_rn(yy, __fmul_rn(1.402f, cr)));
+      a.px[3 * i + 1] = clamp_round(__fadd_rn(__fadd_rn(yy, -__fmul_rn(0.34413f, cb)), -__fmul_rn(0.71414f, cr)));
+      a.px[3 * i + 2] = clamp_round(__fadd_rn(yy, __fmul_rn(1.772f, cb)));
+    } else {
+      for (int c = 0; c < a.ncomp; ++c) a.px[a.ncomp * i + c] = clamp_round(f[c * n + i]);
+    }
+  }
+}
+
 }  // namespace
+
+void launch_decode_reconstruct(const DecodeArgs& a, const std::pair<int, int>* ladder, int levels, cudaStream_t st) {
+  const size_t n = (size_t)a.width * a.height;
+  for (int c = 0; c < a.ncomp; ++c)
+    for (int l = 1; l <= levels; ++l) {
+      const int rw = ladder[l].first, rh = ladder[l].second;
+      if (rw == 0 || rh == 0) continue;
+      const unsigned rows_grid = (unsigned)(((size_t)rh * 32 + 255) / 256), cols_grid = (unsigned)((rw + 127) / 128);
+      if (a.reversible) {
+        int32_t* plane = a.plane + (size_t)c * n;
+        dec53_rows_kernel<<<rows_grid, 256, 0, st>>>(plane, a.tmp, (int)a.width, rw, rh);
+        dec53_cols_kernel<<<cols_grid, 128, 0, st>>>(plane, a.tmp, (int)a.width, rw, rh);
+      } else {
+        float* plane = reinterpret_cast<float*>(a.plane) + (size_t)c * n;
+        float* tmp = reinterpret_cast<float*>(a.tmp);
+        recon_rows_kernel<<<rows_grid, 256, 0, st>>>(plane, tmp, (int)a.width, rw, rh);
+        recon_cols_kernel<<<cols_grid, 128, 0, st>>>(plane, tmp, (int)a.width, rw, rh);
+      }
+    }
+  dec_pixels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
+}
 
 void launch_recon(const ReconArgs& r, const std::pair<int, int>* ladder, int levels, cudaStream_t st) {
   const size_t n = (size_t)r.width * r.height;

@@ -14,6 +14,7 @@ namespace jp2g {
 
 bool upload_t1_tables(const uint8_t* zc, const uint8_t* sc, const uint8_t* spb,
                       const uint32_t* mq);
+bool upload_decode_tables(const uint8_t* zc, const uint8_t* sc, const uint8_t* spb, const uint32_t* mq);
 
 namespace {
 
@@ -103,7 +104,7 @@ bool init_t1_tables() {
   uint8_t zc[2048], sc[256], spb[256];
   uint32_t mq[94];
   build_t1_tables(zc, sc, spb, mq);
-  return upload_t1_tables(zc, sc, spb, mq);
+  return upload_t1_tables(zc, sc, spb, mq) && upload_decode_tables(zc, sc, spb, mq);
 }
 
 }  // namespace jp2g
