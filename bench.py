@@ -23,6 +23,9 @@ Beside the headline, the same run measures the batched and served paths
             5100x6600}, 50% gray / 50% sRGB, quality from {50, 75, 85, 100},
             photo area 0-40%, in one jp2g_encode_batch call per step, against
             one jp2g_encode_device per page (--uneven-pages);
+  decode  : jp2g_decode of 2550x3300 gray q85, sRGB q75 and gray lossless
+            codestreams (host bytes in, samples out), beside the oracle's
+            single-threaded decoder on the same bytes (--no-decode);
   served  : Poisson arrivals of a 70% uneven-page / 30% 256x256 gray q60
             thumbnail mix through jp2g_submit/jp2g_poll under a 40 GB device
             budget: an offered-rate sweep (4 s per rate, extended upward while
@@ -445,6 +448,37 @@ def bench_served(jl, local, args, pool):
             "plain_pages_per_s": plain_pps}
 
 
+def bench_decode(eng, args):
+    """Device decoding (jp2g_decode: host bytes in, interleaved samples out,
+    the host parse and both copies inside the timed region) of 2550x3300
+    codestreams this encoder wrote, against the oracle's single-threaded
+    restatement of the reference's decoder on the same bytes (also the
+    parity check: the samples must be equal)."""
+    from jp2lam_gb300._native import synth_page
+    from tests import oracle_lib
+    orc = oracle_lib.load()
+    legs = {}
+    for name, c, q in (("gray_q85", 1, 85), ("srgb_q75", 3, 75), ("gray_q100", 1, 100)):
+        px = synth_page(W, H, c, 1, photo_w=800, photo_h=600)
+        data = eng.encode(px, W, H, c, q, FMT)
+        for _ in range(max(args.warmup, 1)):
+            got = eng.decode(data)[0]
+        times = []
+        for _ in range(args.decode_steps):
+            t0 = time.perf_counter()
+            got = eng.decode(data)[0]
+            times.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        want = orc.decode(data)[3]
+        cpu_s = time.perf_counter() - t0
+        ms = float(np.median(times)) * 1e3
+        legs[name] = {"e2e_mpix_per_s": W * H / 1e6 / (ms / 1e3), "ms_median": ms,
+                      "ms_min": float(np.min(times)) * 1e3, "bytes": len(data),
+                      "cpu_oracle_mpix_per_s": W * H / 1e6 / cpu_s, "cpu_cores": 1,
+                      "equal_to_oracle": bool(np.array_equal(np.frombuffer(got, np.uint8), want))}
+    return legs
+
+
 def _r(x, nd=1):
     return None if x is None else round(float(x), nd)
 
@@ -467,6 +501,11 @@ def _compact_legs(detail):
         out["uneven"] = {"value": _r(u["value"]), "e2e": _r(u["e2e"]), "unit": "MPix/s",
                          "pages": u["pages"], "pages_per_s": _r(u["pages_per_s"]), "plain": _r(u["plain"]),
                          "speedup_vs_plain": _r(u["speedup_vs_plain"], 2)}
+    d = detail.get("decode")
+    if d:
+        out["decode"] = {k: {"e2e": _r(v["e2e_mpix_per_s"]), "cpu_oracle": _r(v["cpu_oracle_mpix_per_s"]),
+                             "equal": v["equal_to_oracle"]} for k, v in d.items()}
+        out["decode"]["unit"] = "MPix/s"
     v = detail.get("served")
     if v:
         k = v.get("at_knee") or {}
@@ -491,6 +530,9 @@ def main():
     ap.add_argument("--only-batch", action="store_true",
                     help="run only the batched leg (for profiling); prints its object")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-decode", action="store_true")
+    ap.add_argument("--only-decode", action="store_true", help="run only the decode leg; prints its object")
+    ap.add_argument("--decode-steps", type=int, default=10)
     ap.add_argument("--no-autotune", action="store_true",
                     help="time the batched and uneven workloads under the default options")
     ap.add_argument("--batch-pages", type=int, default=64)
@@ -552,6 +594,10 @@ def main():
     if args.only_batch:
         eng.set_timing(True)
         print(json.dumps(bench_batched(eng, stream, torch, f"cuda:{local}", args)), flush=True)
+        eng.close()
+        return
+    if args.only_decode:
+        print(json.dumps(bench_decode(eng, args)), flush=True)
         eng.close()
         return
     dev_fn = lambda: eng.encode_device(d_px.data_ptr(), W, H, NCOMP, QUALITY, FMT)
@@ -666,6 +712,8 @@ def main():
         eng.set_timing(True)
         detail["batched"] = bench_batched(eng, stream, torch, f"cuda:{local}", args)
         detail["uneven"] = bench_uneven(eng, stream, torch, f"cuda:{local}", args, pool)
+    if not args.no_decode and rank == 0:
+        detail["decode"] = bench_decode(eng, args)
     if not args.no_serve:
         detail["served"] = bench_served(jl, local, args, pool)
     if rank == 0:

@@ -81,12 +81,27 @@ int jp2g_encode_with_psnr(jp2g_ctx* ctx, const uint8_t* px, uint32_t w, uint32_t
  * the device. *px (free with jp2g_free) receives w * h * ncomp interleaved
  * samples. Malformed input gives JP2G_DECODE_FAILED, codestreams outside
  * that profile JP2G_UNSUPPORTED_FEATURE, each with a message.
- * flags: JP2G_DECODE_RCT_CHROMA_EXTRA_BITPLANE counts one more magnitude
- * bit-plane for the chroma of reversible RCT codestreams (the encoder codes
- * them with it at quality 100, and QCD does not signal it). */
-enum { JP2G_DECODE_RCT_CHROMA_EXTRA_BITPLANE = 1 };
+ * flags (both off: the reference decoder's behaviour):
+ *   JP2G_DECODE_RCT_CHROMA_EXTRA_BITPLANE counts one more magnitude bit-plane
+ *     for the chroma of reversible RCT codestreams (the encoder codes them
+ *     with it at quality 100, and QCD does not signal it);
+ *   JP2G_DECODE_ACCEPT_EMPTY_SEGMENTS decodes a code-block that has coding
+ *     passes but a segment of zero bytes (which the encoder can emit) from an
+ *     all-0xFF stream instead of failing as decode/t1.rs:109-111 does. */
+enum { JP2G_DECODE_RCT_CHROMA_EXTRA_BITPLANE = 1, JP2G_DECODE_ACCEPT_EMPTY_SEGMENTS = 2 };
 int jp2g_decode(jp2g_ctx* ctx, const uint8_t* bytes, size_t n, int flags, uint8_t** px, size_t* px_len,
                 uint32_t* w, uint32_t* h, uint32_t* ncomp);
+
+/* jp2g_decode over n files at once (bytes[i], lens[i]): the files share
+ * device launches (one Tier-1 decoding launch over all their code-blocks,
+ * one inverse-DWT launch pair per level, one for the samples), in rounds
+ * that fit the device memory budget. Per file: outs[i]/out_lens[i] (free
+ * with jp2g_free), ws/hs/ncomps and status[i]; one file's failure does not
+ * fail the others. Returns JP2G_OK or the first failing file's status (its
+ * message in jp2g_last_error). Samples equal jp2g_decode's for each file. */
+int jp2g_decode_batch(jp2g_ctx* ctx, const uint8_t* const* bytes, const size_t* lens, uint32_t n, int flags,
+                      uint8_t** outs, size_t* out_lens, uint32_t* ws, uint32_t* hs, uint32_t* ncomps,
+                      int* status);
 
 /* Same as jp2g_encode, but `d_px` is interleaved pixel data already resident
  * in device memory (w * h * ncomp bytes). Used for device-resident batching;

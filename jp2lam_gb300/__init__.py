@@ -28,7 +28,7 @@ from ._native import Engine, Jp2LamError, InvalidInput, EncodeFailed, DecodeFail
 __all__ = [
     "ColorSpace", "OutputFormat", "Preset", "Image", "Component", "EncodeOptions",
     "encode", "encode_to_writer", "encode_with_psnr", "EncodeMetrics", "BatchEncoder", "BatchProfile", "encode_batch",
-    "encode_pages", "decode_jp2", "Server", "Engine", "Jp2LamError", "InvalidInput", "EncodeFailed", "DecodeFailed",
+    "encode_pages", "decode_jp2", "decode_batch", "Server", "Engine", "Jp2LamError", "InvalidInput", "EncodeFailed", "DecodeFailed",
     "UnsupportedFeature", "IoError",
 ]
 
@@ -171,16 +171,32 @@ def encode_with_psnr(image: Image, options: EncodeOptions,
 
 
 def decode_jp2(data: bytes, engine: Optional[Engine] = None,
-               rct_chroma_extra_bitplane: bool = False) -> Image:
+               rct_chroma_extra_bitplane: bool = False, accept_empty_segments: bool = False) -> Image:
     """Decode a J2K/JP2 file of this encoder's profile on the GPU
     (decode_jp2, src/decode/mod.rs:56-61). rct_chroma_extra_bitplane counts
     the extra chroma bit-plane that lossless sRGB encodes use and QCD does not
-    signal; without it such files can fail as they do in the reference."""
+    signal; accept_empty_segments decodes code-blocks that have passes but no
+    bytes. Without them such files fail as they do in the reference."""
     eng = engine or default_engine()
-    px, w, h, c = eng.decode(data, rct_chroma_extra_bitplane)
+    px, w, h, c = eng.decode(data, rct_chroma_extra_bitplane, accept_empty_segments)
     if c == 1:
         return Image.from_gray_bytes(w, h, px)
     return Image.from_rgb_bytes(w, h, px)
+
+
+def decode_batch(files, engine: Optional[Engine] = None, rct_chroma_extra_bitplane: bool = False,
+                 accept_empty_segments: bool = False):
+    """decode_jp2 over many files in shared device launches: per file an
+    Image, or the Jp2LamError it failed with."""
+    eng = engine or default_engine()
+    out = []
+    for r in eng.decode_batch(files, rct_chroma_extra_bitplane, accept_empty_segments):
+        if isinstance(r, Jp2LamError):
+            out.append(r)
+        else:
+            px, w, h, c = r
+            out.append(Image.from_gray_bytes(w, h, px) if c == 1 else Image.from_rgb_bytes(w, h, px))
+    return out
 
 
 @dataclass(frozen=True)

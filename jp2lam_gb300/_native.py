@@ -53,6 +53,7 @@ EXPORTS = [
     "jp2g_encode_batch", "jp2g_submit", "jp2g_poll", "jp2g_set_option", "jp2g_get_option",
     "jp2g_autotune", "jp2g_debug_assemble", "jp2g_debug_plan", "jp2g_cancel", "jp2g_debug_context_labels",
     "jp2g_debug_coefficients_f32", "jp2g_encode_with_psnr", "jp2g_debug_assemble_device", "jp2g_decode",
+    "jp2g_decode_batch",
 ]
 
 PENDING = 6
@@ -114,6 +115,9 @@ def load_library(path: str = LIB_PATH):
                                     ctypes.POINTER(_u8p), ctypes.POINTER(ctypes.c_size_t),
                                     ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
                                     ctypes.POINTER(ctypes.c_uint32)]
+        lib.jp2g_decode_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                          ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         lib.jp2g_debug_blocks.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint8,
                                           ctypes.c_void_p, ctypes.c_uint32,
@@ -214,21 +218,55 @@ class Engine:
         self.lib.jp2g_free(out)
         return data, psnr.value, ssim.value
 
-    def decode(self, data: bytes, rct_chroma_extra_bitplane: bool = False):
+    @staticmethod
+    def _decode_flags(rct_chroma_extra_bitplane, accept_empty_segments):
+        return (1 if rct_chroma_extra_bitplane else 0) | (2 if accept_empty_segments else 0)
+
+    def decode(self, data: bytes, rct_chroma_extra_bitplane: bool = False, accept_empty_segments: bool = False):
         """(pixels, w, h, ncomp): a J2K/JP2 file decoded on the device
-        (decode_jp2, src/decode/mod.rs:56-61); pixels interleaved."""
+        (decode_jp2, src/decode/mod.rs:56-61); pixels interleaved. The two
+        options relax the reference decoder's checks (include/jp2g.h)."""
         buf = np.frombuffer(bytes(data), dtype=np.uint8)
         out = _u8p()
         n = ctypes.c_size_t()
         w, h, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
         with self._lock:
             rc = self.lib.jp2g_decode(self.handle, buf.ctypes.data_as(ctypes.c_void_p), buf.size,
-                                      1 if rct_chroma_extra_bitplane else 0, ctypes.byref(out), ctypes.byref(n),
+                                      self._decode_flags(rct_chroma_extra_bitplane, accept_empty_segments),
+                                      ctypes.byref(out), ctypes.byref(n),
                                       ctypes.byref(w), ctypes.byref(h), ctypes.byref(c))
             self._check(rc)
         px = ctypes.string_at(out, n.value)
         self.lib.jp2g_free(out)
         return px, w.value, h.value, c.value
+
+    def decode_batch(self, files, rct_chroma_extra_bitplane: bool = False, accept_empty_segments: bool = False):
+        """jp2g_decode_batch: a list with, per file, (pixels, w, h, ncomp) or
+        the Jp2LamError it failed with."""
+        n = len(files)
+        if n == 0:
+            return []
+        keep = [np.frombuffer(bytes(f), dtype=np.uint8) for f in files]
+        ptrs = (ctypes.c_void_p * n)(*[k.ctypes.data for k in keep])
+        lens = (ctypes.c_size_t * n)(*[k.size for k in keep])
+        outs = (ctypes.c_void_p * n)()
+        out_lens = (ctypes.c_size_t * n)()
+        ws, hs, cs = (ctypes.c_uint32 * n)(), (ctypes.c_uint32 * n)(), (ctypes.c_uint32 * n)()
+        status = (ctypes.c_int * n)()
+        with self._lock:
+            self.lib.jp2g_decode_batch(self.handle, ptrs, lens, n,
+                                       self._decode_flags(rct_chroma_extra_bitplane, accept_empty_segments), outs,
+                                       out_lens, ws, hs, cs, status)
+            msg = self.lib.jp2g_last_error(self.handle)
+            msg = msg.decode() if isinstance(msg, bytes) else str(msg)
+        res = []
+        for i in range(n):
+            if status[i] == 0:
+                res.append((ctypes.string_at(outs[i], out_lens[i]), ws[i], hs[i], cs[i]))
+                self.lib.jp2g_free(ctypes.cast(outs[i], _u8p))
+            else:
+                res.append(_BY_CODE.get(status[i], EncodeFailed)(msg))
+        return res
 
     def encode_device(self, dev_ptr: int, w: int, h: int, ncomp: int, quality: int, fmt: int) -> bytes:
         out = _u8p()

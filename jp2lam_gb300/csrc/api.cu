@@ -1259,8 +1259,9 @@ static int page_metrics(jp2g_ctx* c, const PageJob& j, double* psnr, double* ssi
         r.step = p.quants[g.quant].step_f32;
       }
   const size_t n = (size_t)p.width * p.height;
-  if (!reserve(c, c->recon, (n * (p.ncomp + 3) + 64) * sizeof(float) + 16) ||
-      !reserve(c, c->reconblk, std::max<size_t>(rb.size(), 1) * sizeof(ReconBlock)) ||
+  const size_t rb_bytes = (std::max<size_t>(rb.size(), 1) * sizeof(ReconBlock) + 255) & ~size_t(255);
+  if (!reserve(c, c->recon, (n * (2 * p.ncomp + 2) + 64) * sizeof(float) + 16) ||
+      !reserve(c, c->reconblk, rb_bytes + (size_t)(p.ncomp * p.levels + 1) * sizeof(IdwtJob)) ||
       !cuda_ok(c, cudaMemcpyAsync(c->reconblk.p, rb.data(), rb.size() * sizeof(ReconBlock), cudaMemcpyHostToDevice,
                                   c->stream), "H2D metrics blocks"))
     return kEncodeFailed;
@@ -1281,7 +1282,8 @@ static int page_metrics(jp2g_ctx* c, const PageJob& j, double* psnr, double* ssi
   r.stats = reinterpret_cast<double*>(f);  // 16 bytes at the start
   r.plane = f + 4;
   r.tmp = r.plane + n * p.ncomp;
-  r.luma_orig = r.tmp + n;
+  r.jobs = reinterpret_cast<IdwtJob*>(static_cast<uint8_t*>(c->reconblk.p) + rb_bytes);
+  r.luma_orig = r.tmp + n * p.ncomp;
   r.luma_dec = r.luma_orig + n;
   launch_recon(r, p.ladder.data(), p.levels, c->stream);
   double sums[2] = {0, 0};
@@ -1317,63 +1319,237 @@ int jp2g_encode_with_psnr(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h
   return finish_output(c, rc, j, out, out_len);
 }
 
-// decode_jp2 (src/decode/mod.rs:56-61) on the device: the host parses the
-// boxes, headers and packet headers (decode.cpp); the code-blocks are decoded
-// and the image reconstructed by kernels (t1dec.cu, recon.cu).
+// ------------------------------------------------------------- decoding --
+// decode_jp2 (src/decode/mod.rs:56-61) on the device, for many files at
+// once: the host parses each file's boxes, headers and packet headers
+// (decode.cpp, on host threads); a round of files then shares one Tier-1
+// decoding launch over all their code-blocks, one inverse-DWT launch pair
+// per level over all their components, and one launch for the samples
+// (t1dec.cu, recon.cu). Rounds are sized by device memory (the context's
+// budget, else 8 GiB of planes); a round that does not fit is split.
+namespace {
+
+struct DecodePage {
+  DecodeLayout L;
+  int status = JP2G_OK;
+  std::string msg;
+  uint64_t npx = 0;
+  uint64_t data_base = 0, plane_base = 0, px_base = 0;
+};
+
+uint64_t decode_device_bytes(const DecodePage& p, size_t nbytes) {
+  // bytes, planes, tmp planes, samples, code-blocks, jobs
+  return nbytes + p.npx * p.L.ncomp * 9 + p.L.blocks.size() * sizeof(DecBlock) +
+         (uint64_t)(p.L.levels * p.L.ncomp + 1) * sizeof(IdwtJob) + sizeof(PixJob) + 1024;
+}
+
+// Decodes the pages `ids` in one device round; fills outs / out_lens.
+int decode_round(jp2g_ctx* c, std::vector<DecodePage>& pg, const std::vector<size_t>& ids,
+                 const uint8_t* const* bytes, const size_t* lens, uint8_t** outs, size_t* out_lens) {
+  uint64_t nbytes = 0, nplane = 0, npxb = 0, nblk = 0;
+  int maxl = 0;
+  for (size_t i : ids) {
+    DecodePage& p = pg[i];
+    p.data_base = nbytes;
+    p.plane_base = nplane;
+    p.px_base = npxb;
+    nbytes += (lens[i] + 15) & ~size_t(15);
+    nplane += p.npx * p.L.ncomp;
+    npxb += p.npx * p.L.ncomp;
+    nblk += p.L.blocks.size();
+    maxl = std::max(maxl, p.L.levels);
+  }
+  if (nbytes > 0xffffffffull) return set_err(c, JP2G_INVALID_INPUT, "decode round exceeds 4 GiB of input");
+  // device job tables: blocks, then per-level inverse-DWT jobs, then pixel jobs
+  std::vector<DecBlock> blk;
+  blk.reserve(nblk);
+  for (size_t i : ids)
+    for (DecBlock b : pg[i].L.blocks) {
+      b.plane_off += pg[i].plane_base;
+      b.data_off += (uint32_t)pg[i].data_base;
+      blk.push_back(b);
+    }
+  const size_t planes_bytes = (size_t)nplane * 4;
+  if (!reserve(c, c->t2out, std::max<uint64_t>(nbytes, 16)) ||
+      !reserve(c, c->recon, planes_bytes * 2 + (size_t)npxb + 256))
+    return JP2G_DECODE_FAILED;
+  int32_t* planes = dptr<int32_t>(c->recon);
+  int32_t* tmp = planes + nplane;
+  uint8_t* dpx = reinterpret_cast<uint8_t*>(tmp + nplane);
+  std::vector<IdwtJob> jobs;
+  std::vector<uint32_t> first(maxl + 2, 0), rows(maxl + 2, 0), tiles(maxl + 2, 0);
+  for (int l = 1; l <= maxl; ++l) {
+    first[l] = (uint32_t)jobs.size();
+    for (size_t i : ids) {
+      const DecodePage& p = pg[i];
+      if (p.L.levels < l) continue;
+      const uint32_t rw = (uint32_t)p.L.ladder[l].first, rh = (uint32_t)p.L.ladder[l].second;
+      for (int comp = 0; comp < p.L.ncomp; ++comp) {
+        IdwtJob j{};
+        j.plane = planes + p.plane_base + (uint64_t)comp * p.npx;
+        j.tmp = tmp + p.plane_base + (uint64_t)comp * p.npx;
+        j.stride = p.L.width;
+        j.rw = rw;
+        j.rh = rh;
+        j.reversible = p.L.reversible ? 1u : 0u;
+        j.row_base = rows[l];
+        j.tile_base = tiles[l];
+        rows[l] += rh;
+        tiles[l] += ((rw + 31) / 32) * ((rh + kIdwtTileRows - 1) / kIdwtTileRows);
+        jobs.push_back(j);
+      }
+    }
+  }
+  first[maxl + 1] = (uint32_t)jobs.size();
+  std::vector<PixJob> pix;
+  uint64_t total_px = 0;
+  for (size_t i : ids) {
+    const DecodePage& p = pg[i];
+    PixJob j{};
+    j.planes = planes + p.plane_base;
+    j.px = dpx + p.px_base;
+    j.npx = p.npx;
+    j.pix_base = total_px;
+    j.ncomp = (uint32_t)p.L.ncomp;
+    j.mct = p.L.mct ? 1u : 0u;
+    j.reversible = p.L.reversible ? 1u : 0u;
+    total_px += p.npx;
+    pix.push_back(j);
+  }
+  const size_t blk_bytes = (blk.size() * sizeof(DecBlock) + 255) & ~size_t(255);
+  const size_t job_bytes = (jobs.size() * sizeof(IdwtJob) + 255) & ~size_t(255);
+  if (!reserve(c, c->reconblk, blk_bytes + job_bytes + pix.size() * sizeof(PixJob) + 256) ||
+      !reserve_host(c, c->hpx, std::max<uint64_t>(nbytes, 16)) || !reserve_host(c, c->hout, std::max<uint64_t>(npxb, 16)))
+    return JP2G_DECODE_FAILED;
+  uint8_t* meta = static_cast<uint8_t*>(c->reconblk.p);
+  DecBlock* dblk = reinterpret_cast<DecBlock*>(meta);
+  IdwtJob* djobs = reinterpret_cast<IdwtJob*>(meta + blk_bytes);
+  PixJob* dpix = reinterpret_cast<PixJob*>(meta + blk_bytes + job_bytes);
+  parallel_for(ids.size(), ids.size() >= 8 ? host_threads(c) : 1,
+               [&](size_t k) { std::memcpy(static_cast<uint8_t*>(c->hpx.p) + pg[ids[k]].data_base, bytes[ids[k]], lens[ids[k]]); });
+  if (!cuda_ok(c, cudaMemcpyAsync(c->t2out.p, c->hpx.p, nbytes, cudaMemcpyHostToDevice, c->stream), "H2D files") ||
+      (!blk.empty() && !cuda_ok(c, cudaMemcpyAsync(dblk, blk.data(), blk.size() * sizeof(DecBlock),
+                                                   cudaMemcpyHostToDevice, c->stream), "H2D code-blocks")) ||
+      (!jobs.empty() && !cuda_ok(c, cudaMemcpyAsync(djobs, jobs.data(), jobs.size() * sizeof(IdwtJob),
+                                                    cudaMemcpyHostToDevice, c->stream), "H2D jobs")) ||
+      !cuda_ok(c, cudaMemcpyAsync(dpix, pix.data(), pix.size() * sizeof(PixJob), cudaMemcpyHostToDevice, c->stream),
+               "H2D pages") ||
+      !cuda_ok(c, cudaMemsetAsync(planes, 0, planes_bytes, c->stream), "memset planes"))
+    return JP2G_DECODE_FAILED;
+  launch_t1_decode(dblk, (uint32_t)blk.size(), dptr<uint8_t>(c->t2out), planes, c->stream);
+  for (int l = 1; l <= maxl; ++l) launch_idwt_level(djobs + first[l], first[l + 1] - first[l], rows[l], tiles[l], c->stream);
+  launch_dec_pixels(dpix, (uint32_t)pix.size(), total_px, c->stream);
+  if (!cuda_ok(c, cudaGetLastError(), "decode kernels") ||
+      !cuda_ok(c, cudaMemcpyAsync(c->hout.p, dpx, npxb, cudaMemcpyDeviceToHost, c->stream), "D2H samples") ||
+      !cuda_ok(c, cudaStreamSynchronize(c->stream), "decode"))
+    return JP2G_DECODE_FAILED;
+  std::atomic<bool> oom{false};
+  parallel_for(ids.size(), ids.size() >= 8 && npxb >= (8u << 20) ? host_threads(c) : 1, [&](size_t k) {
+    const DecodePage& p = pg[ids[k]];
+    const size_t len = (size_t)p.npx * p.L.ncomp;
+    uint8_t* o = static_cast<uint8_t*>(std::malloc(std::max<size_t>(len, 1)));
+    if (!o) {
+      oom = true;
+      return;
+    }
+    std::memcpy(o, static_cast<const uint8_t*>(c->hout.p) + p.px_base, len);
+    outs[ids[k]] = o;
+    out_lens[ids[k]] = len;
+  });
+  if (oom) return set_err(c, JP2G_DECODE_FAILED, "out of host memory");
+  return JP2G_OK;
+}
+
+// Splits `ids` into rounds that fit, halving a round whose pools could not
+// grow within the budget.
+int decode_rounds(jp2g_ctx* c, std::vector<DecodePage>& pg, std::vector<size_t> ids, const uint8_t* const* bytes,
+                  const size_t* lens, uint8_t** outs, size_t* out_lens) {
+  const uint64_t cap = c->budget ? c->budget : (uint64_t)9 << 30;
+  size_t k = 0;
+  while (k < ids.size()) {
+    std::vector<size_t> round;
+    uint64_t used = 0;
+    while (k < ids.size()) {
+      const uint64_t b = decode_device_bytes(pg[ids[k]], lens[ids[k]]);
+      if (!round.empty() && used + b > cap) break;
+      used += b;
+      round.push_back(ids[k++]);
+    }
+    c->budget_hit = false;
+    int rc = decode_round(c, pg, round, bytes, lens, outs, out_lens);
+    if (rc != JP2G_OK && c->budget_hit && round.size() > 1) {
+      release_pools(c);
+      const size_t half = round.size() / 2;
+      std::vector<size_t> a(round.begin(), round.begin() + half), b(round.begin() + half, round.end());
+      rc = decode_rounds(c, pg, a, bytes, lens, outs, out_lens);
+      if (rc == JP2G_OK) rc = decode_rounds(c, pg, b, bytes, lens, outs, out_lens);
+    }
+    if (rc != JP2G_OK) {
+      const std::string m = get_msg(c);
+      for (size_t i : round)
+        if (!outs[i] && pg[i].status == JP2G_OK) {
+          pg[i].status = rc;
+          pg[i].msg = m;
+        }
+    }
+  }
+  return JP2G_OK;
+}
+
+}  // namespace
+
+int jp2g_decode_batch(jp2g_ctx* c, const uint8_t* const* bytes, const size_t* lens, uint32_t n, int flags,
+                      uint8_t** outs, size_t* out_lens, uint32_t* ws, uint32_t* hs, uint32_t* ncomps, int* status) {
+  if (!c) return JP2G_INVALID_INPUT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (n == 0) return JP2G_OK;
+  if (!bytes || !lens || !outs || !out_lens || !ws || !hs || !ncomps || !status)
+    return set_err(c, JP2G_INVALID_INPUT, "array pointer is null");
+  cudaSetDevice(c->device);
+  std::vector<DecodePage> pg(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    outs[i] = nullptr;
+    out_lens[i] = 0;
+    ws[i] = hs[i] = ncomps[i] = 0;
+  }
+  parallel_for(n, n >= 4 ? host_threads(c) : 1, [&](size_t i) {
+    DecodePage& p = pg[i];
+    Failure f{};
+    if (!bytes[i] && lens[i]) {
+      p.status = JP2G_INVALID_INPUT;
+      p.msg = "input pointer is null";
+    } else if (!parse_codestream(bytes[i], lens[i], flags, &p.L, &f)) {
+      p.status = f.code;
+      p.msg = f.msg;
+    } else {
+      p.npx = (uint64_t)p.L.width * p.L.height;
+    }
+  });
+  std::vector<size_t> ok;
+  for (uint32_t i = 0; i < n; ++i)
+    if (pg[i].status == JP2G_OK) ok.push_back(i);
+  decode_rounds(c, pg, ok, bytes, lens, outs, out_lens);
+  int first = JP2G_OK;
+  for (uint32_t i = 0; i < n; ++i) {
+    status[i] = pg[i].status;
+    if (pg[i].status == JP2G_OK) {
+      ws[i] = pg[i].L.width;
+      hs[i] = pg[i].L.height;
+      ncomps[i] = (uint32_t)pg[i].L.ncomp;
+    } else if (first == JP2G_OK) {
+      first = pg[i].status;
+      set_msg(c, pg[i].msg);
+    }
+  }
+  return first;
+}
+
 int jp2g_decode(jp2g_ctx* c, const uint8_t* bytes, size_t n, int flags, uint8_t** px, size_t* px_len, uint32_t* w,
                 uint32_t* h, uint32_t* ncomp) {
   if (!c) return JP2G_INVALID_INPUT;
-  std::lock_guard<std::mutex> lk(c->mu);
   if (!px || !px_len || !w || !h || !ncomp) return set_err(c, JP2G_INVALID_INPUT, "output pointer is null");
-  if (!bytes && n) return set_err(c, JP2G_INVALID_INPUT, "input pointer is null");
-  cudaSetDevice(c->device);
-  DecodeLayout L;
-  Failure f{};
-  if (!parse_codestream(bytes, n, (flags & JP2G_DECODE_RCT_CHROMA_EXTRA_BITPLANE) != 0, &L, &f))
-    return set_err(c, f.code, f.msg);
-  const uint64_t npx = (uint64_t)L.width * L.height;
-  if (npx > (1ull << 30)) return set_err(c, JP2G_UNSUPPORTED_FEATURE, "image too large to decode");
-  const size_t plane_bytes = (size_t)npx * L.ncomp * 4, out_bytes = (size_t)npx * L.ncomp;
-  const size_t nb = L.blocks.size();
-  if (!reserve(c, c->t2out, std::max<size_t>(n, 16)) ||
-      !reserve(c, c->reconblk, std::max<size_t>(nb, 1) * sizeof(DecBlock)) ||
-      !reserve(c, c->recon, plane_bytes + (size_t)npx * 4 + out_bytes + 256))
-    return JP2G_DECODE_FAILED;
-  DecodeArgs a{};
-  a.data = dptr<uint8_t>(c->t2out);
-  a.blocks = dptr<DecBlock>(c->reconblk);
-  a.nblocks = (uint32_t)nb;
-  a.width = L.width;
-  a.height = L.height;
-  a.ncomp = L.ncomp;
-  a.reversible = L.reversible;
-  a.mct = L.mct;
-  a.plane = dptr<int32_t>(c->recon);
-  a.tmp = a.plane + npx * L.ncomp;
-  a.px = reinterpret_cast<uint8_t*>(a.tmp + npx);
-  uint8_t* out = static_cast<uint8_t*>(std::malloc(std::max<size_t>(out_bytes, 1)));
-  if (!out) return set_err(c, JP2G_DECODE_FAILED, "out of host memory");
-  if (!cuda_ok(c, cudaMemcpyAsync(c->t2out.p, bytes, n, cudaMemcpyHostToDevice, c->stream), "H2D codestream") ||
-      !cuda_ok(c, cudaMemcpyAsync(c->reconblk.p, L.blocks.data(), nb * sizeof(DecBlock), cudaMemcpyHostToDevice,
-                                  c->stream), "H2D code-blocks") ||
-      !cuda_ok(c, cudaMemsetAsync(a.plane, 0, plane_bytes, c->stream), "memset planes")) {
-    std::free(out);
-    return JP2G_DECODE_FAILED;
-  }
-  launch_t1_decode(a, c->stream);
-  launch_decode_reconstruct(a, L.ladder.data(), L.levels, c->stream);
-  if (!cuda_ok(c, cudaGetLastError(), "decode kernels") ||
-      !cuda_ok(c, cudaMemcpyAsync(out, a.px, out_bytes, cudaMemcpyDeviceToHost, c->stream), "D2H samples") ||
-      !cuda_ok(c, cudaStreamSynchronize(c->stream), "decode")) {
-    std::free(out);
-    return JP2G_DECODE_FAILED;
-  }
-  *px = out;
-  *px_len = out_bytes;
-  *w = L.width;
-  *h = L.height;
-  *ncomp = (uint32_t)L.ncomp;
-  return JP2G_OK;
+  int st = JP2G_OK;
+  return jp2g_decode_batch(c, &bytes, &n, 1, flags, px, px_len, w, h, ncomp, &st);
 }
 
 static void job_from_request(const jp2g_request& r, PageJob* j) {

@@ -128,8 +128,8 @@ bool fail(Failure* err, int code, const char* msg) {
 
 }  // namespace
 
-bool parse_codestream(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane, DecodeLayout* out,
-                      Failure* err) {
+bool parse_codestream(const uint8_t* bytes, size_t n, int flags, DecodeLayout* out, Failure* err) {
+  const bool rct_chroma_extra_bitplane = (flags & 1) != 0, accept_empty = (flags & 2) != 0;
   // JP2 boxes: the codestream is the jp2c box (src/decode/jp2_parse.rs)
   size_t cs0 = 0, csn = n;
   if (n >= 12 && bytes[4] == 'j' && bytes[5] == 'P') {
@@ -214,6 +214,7 @@ bool parse_codestream(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitp
   }
   if (L.width == 0 || L.height == 0 || (L.ncomp != 1 && L.ncomp != 3) || L.precision != 8)
     return fail(err, kUnsupportedFeature, "only 8-bit gray or 3-component codestreams are decoded");
+  if ((uint64_t)L.width * L.height > (1ull << 30)) return fail(err, kUnsupportedFeature, "image too large to decode");
   if (L.levels > 32 || L.cbw > 64 || L.cbh > 64)
     return fail(err, kUnsupportedFeature, "unsupported coding parameters");
   // resolution ladder (index 0 = the smallest) and band rectangles
@@ -260,12 +261,13 @@ bool parse_codestream(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitp
         for (int i = 0; i < ncbx * ncby; ++i) {
           DecBlock b{};
           const int bx = i % ncbx, by = i / ncbx;
-          b.x0 = (uint32_t)(rc.x0 + bx * L.cbw);
-          b.y0 = (uint32_t)(rc.y0 + by * L.cbh);
-          b.w = (uint16_t)(std::min(rc.x0 + (bx + 1) * L.cbw, rc.x1) - (int)b.x0);
-          b.h = (uint16_t)(std::min(rc.y0 + (by + 1) * L.cbh, rc.y1) - (int)b.y0);
-          b.comp = (uint8_t)comp;
+          const int x0 = rc.x0 + bx * L.cbw, y0 = rc.y0 + by * L.cbh;
+          b.plane_off = ((uint64_t)comp * L.height + (uint64_t)y0) * L.width + (uint64_t)x0;
+          b.stride = L.width;
+          b.w = (uint16_t)(std::min(x0 + L.cbw, rc.x1) - x0);
+          b.h = (uint16_t)(std::min(y0 + L.cbh, rc.y1) - y0);
           b.orient = (uint8_t)rc.orient;
+          b.reversible = L.reversible ? 1 : 0;
           b.mb = (uint8_t)std::max(0, std::min(mb, 255));
           b.step = step;
           if (incl.below(hb, i, 1)) {
@@ -303,7 +305,8 @@ bool parse_codestream(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitp
         b.data_off = (uint32_t)body;
         body += b.data_len;
         // decode/t1.rs:87-130: bit-planes from QCD, the pass-count limit
-        if (b.data_len == 0) return fail(err, kDecodeFailed, "non-empty code-block has no compressed bytes");
+        if (b.data_len == 0 && !accept_empty)
+          return fail(err, kDecodeFailed, "non-empty code-block has no compressed bytes");
         if (b.zbp > b.mb) return fail(err, kDecodeFailed, "zero-bitplane count exceeds subband bit-plane count");
         const int mbp = b.mb - b.zbp;
         if (mbp == 0) return fail(err, kDecodeFailed, "non-empty code-block has no magnitude bit-planes");

@@ -168,16 +168,20 @@ void launch_t2(const T2Args& a, uint32_t* scan_scratch, int num_sms, cudaStream_
 // ------------------------------------------------------------- decoding --
 // One code-block of a codestream being decoded.
 struct DecBlock {
+  uint64_t plane_off;           // its first sample in the planes buffer (elements)
   uint32_t data_off, data_len;  // its segment in the input bytes
-  uint32_t x0, y0;              // its samples in its component's plane (Mallat layout)
+  uint32_t stride;              // its plane's row pitch (the image width)
   uint16_t w, h;
-  uint8_t comp, orient, mb, zbp;  // mb: bit-planes from QCD (decode/t1.rs:56)
+  uint8_t orient, mb, zbp;  // mb: bit-planes from QCD (decode/t1.rs:56)
+  uint8_t reversible;       // 1: signed integers out, 0: dequantised f32 bits
   uint16_t npasses;
   uint16_t pad;
   float step;  // quantiser step (irreversible codestreams)
 };
 
-// What the host parse learns from a codestream (decode.cpp).
+// What the host parse learns from a codestream (decode.cpp). Block
+// plane_off and data_off are relative to the page's planes (component c at
+// c * width * height) and to the start of its bytes.
 struct DecodeLayout {
   uint32_t width = 0, height = 0;
   int ncomp = 0, precision = 0, levels = 0, cbw = 64, cbh = 64, guard = 2;
@@ -185,24 +189,37 @@ struct DecodeLayout {
   std::vector<std::pair<int, int>> ladder;  // resolution sizes, index 0 = the smallest
   std::vector<DecBlock> blocks;
 };
-bool parse_codestream(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane, DecodeLayout* out,
-                      Failure* err);
+// flags: bit 0 one more magnitude bit-plane for RCT chroma, bit 1 accept
+// code-blocks whose segment has zero bytes (the JP2G_DECODE_* flags).
+bool parse_codestream(const uint8_t* bytes, size_t n, int flags, DecodeLayout* out, Failure* err);
 
-struct DecodeArgs {
-  const uint8_t* data;  // the input bytes on the device
-  const DecBlock* blocks;
-  uint32_t nblocks;
-  uint32_t width, height;
-  int ncomp, reversible, mct;
-  int32_t* plane;  // ncomp planes of width * height: int32 coefficients, or f32 values when irreversible
-  int32_t* tmp;    // one plane of scratch
-  uint8_t* px;     // width * height * ncomp interleaved output samples
+// One component of one page at one inverse-DWT level: its planes hold
+// int32 (5/3) or f32 (9/7) samples, rows `stride` apart; the level's
+// rw x rh region is transformed rows first (plane -> tmp), then columns
+// (tmp -> plane). row_base / tile_base: the job's first global row and
+// first 32-column tile in the level's launch.
+struct IdwtJob {
+  void* plane;
+  void* tmp;
+  uint32_t stride, rw, rh, reversible;
+  uint32_t row_base, tile_base;
 };
-// Tier-1 decoding of every code-block (t1dec.cu), then dequantisation,
-// the inverse DWT per component, inverse RCT/ICT and the 8-bit samples
-// (recon.cu). plane must be zeroed before.
-void launch_t1_decode(const DecodeArgs& a, cudaStream_t st);
-void launch_decode_reconstruct(const DecodeArgs& a, const std::pair<int, int>* ladder, int levels, cudaStream_t st);
+// One page's final samples: inverse RCT/ICT (when mct and 3 components),
+// level shift and clamp into interleaved 8-bit samples.
+struct PixJob {
+  const int32_t* planes;  // ncomp planes of npx samples (int32 or f32 bits)
+  uint8_t* px;
+  uint64_t npx, pix_base;  // pix_base: the page's first global sample index
+  uint32_t ncomp, mct, reversible, pad;
+};
+// Tier-1 decoding of every code-block (t1dec.cu) into zeroed planes.
+void launch_t1_decode(const DecBlock* blocks, uint32_t nblocks, const uint8_t* data, int32_t* planes,
+                      cudaStream_t st);
+// One inverse-DWT level for njobs jobs (recon.cu).
+void launch_idwt_level(const IdwtJob* jobs, uint32_t njobs, uint32_t total_rows, uint32_t total_tiles,
+                       cudaStream_t st);
+constexpr int kIdwtTileRows = 64;  // rows per column tile of launch_idwt_level
+void launch_dec_pixels(const PixJob* jobs, uint32_t njobs, uint64_t total_px, cudaStream_t st);
 bool upload_decode_tables(const uint8_t* zc, const uint8_t* sc, const uint8_t* spb, const uint32_t* mq);
 
 // Where a code-block's samples sit in its component's plane (Mallat
@@ -226,7 +243,8 @@ struct ReconArgs {
   int ncomp;
   const uint8_t* px;  // the page's interleaved pixels on the device
   float* plane;       // ncomp planes of width * height
-  float* tmp;         // one plane of scratch
+  float* tmp;         // ncomp planes of scratch
+  IdwtJob* jobs;      // device room for ncomp * levels inverse-DWT jobs
   float* luma_orig;
   float* luma_dec;
   double* stats;      // [0] sum of squared errors, [1] sum of 8x8 block SSIMs

@@ -13,6 +13,8 @@
 // the oracle's; only the f64 sums run in a different order.
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "jp2g_internal.h"
 #include "kernels.h"
 
@@ -65,59 +67,143 @@ __device__ __forceinline__ float lifted(float x, float c, float l, float rr) {
   return __fadd_rn(x, __fmul_rn(c, __fadd_rn(l, rr)));
 }
 
-// Inverse 1-D 9/7 of row y (rw samples, low half first): a warp per row,
-// each step's positions in parallel, through the row's slice of `tmp`.
-__global__ void recon_rows_kernel(float* plane, float* tmp, int stride, int rw, int rh) {
-  const int lane = threadIdx.x & 31;
-  const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (y >= rh) return;
-  float* x = plane + (size_t)y * stride;
-  float* t = tmp + (size_t)y * stride;
-  const int n = rw;
-  if (n < 2) {
-    if (n == 1 && lane == 0) x[0] = __fmul_rn(x[0], kRK);
-    return;
+// The job holding global index g (rows or tiles) of a level's launch.
+__device__ __forceinline__ const IdwtJob& job_of(const IdwtJob* jobs, uint32_t njobs, uint32_t g, bool tiles) {
+  uint32_t lo = 0, hi = njobs;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if ((tiles ? jobs[mid].tile_base : jobs[mid].row_base) <= g) lo = mid;
+    else hi = mid;
   }
-  const int sn = (n + 1) / 2;
-  for (int i = lane; i < n; i += 32) {
-    const float v = i & 1 ? x[sn + (i >> 1)] : x[i >> 1];
-    t[i] = __fmul_rn(v, i & 1 ? kRInvK : kRK);
-  }
-  __syncwarp();
-  const float c[4] = {-kRDelta, -kRGamma, -kRBeta, -kRAlpha};
-  #pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    for (int j = (s & 1) + 2 * lane; j < n; j += 64)
-      t[j] = lifted(t[j], c[s], t[sym_at(j - 1, n)], t[sym_at(j + 1, n)]);
-    __syncwarp();
-  }
-  for (int i = lane; i < n; i += 32) x[i] = t[i];
+  return jobs[lo];
 }
 
-// Inverse 1-D 9/7 of every column x < rw over rh rows: a thread per column
-// (neighbouring threads read neighbouring samples of a row), through `tmp`.
-__global__ void recon_cols_kernel(float* plane, float* tmp, int stride, int rw, int rh) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= rw) return;
-  float* p = plane + x;
-  float* t = tmp + x;
-  const int n = rh;
-  if (n < 2) {
-    if (n == 1) p[0] = __fmul_rn(p[0], kRK);
-    return;
+// Inverse 1-D transform of one row (rw samples, low half first) of a job's
+// plane into the same row of its tmp, interleaved: a warp per row, each
+// lifting step's positions in parallel.
+//  9/7 (src/dwt/irrev97.rs:639-796): scale by K / 1/K, then the four
+//    lifting steps x[j] += c (x[j-1] + x[j+1]) over whole-sample symmetric
+//    extension, each rounded as written.
+//  5/3 (src/dwt/rev53.rs:96-129, 419-497): even samples
+//    s[i] - ((d[i-1] + d[i] + 2) >> 2) with the edges clamped, then odd
+//    samples d[i] + ((e[i] + e[i+1]) >> 1), or d[i] + e[i] at the right edge.
+__global__ void idwt_rows_kernel(const IdwtJob* jobs, uint32_t njobs, uint32_t total_rows) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (g >= total_rows) return;
+  const IdwtJob& jb = job_of(jobs, njobs, g, false);
+  const uint32_t y = g - jb.row_base;
+  const int n = (int)jb.rw, sn = (n + 1) / 2, dn = n - sn;
+  if (jb.reversible) {
+    const int32_t* x = static_cast<const int32_t*>(jb.plane) + (size_t)y * jb.stride;
+    int32_t* t = static_cast<int32_t*>(jb.tmp) + (size_t)y * jb.stride;
+    if (n == 1) {
+      if (lane == 0) t[0] = x[0];
+      return;
+    }
+    for (int i = lane; i < sn; i += 32) {
+      const int l = min(max(i - 1, 0), dn - 1), r = min(i, dn - 1);
+      t[2 * i] = x[i] - ((x[sn + l] + x[sn + r] + 2) >> 2);
+    }
+    __syncwarp();
+    for (int i = lane; i < dn; i += 32)
+      t[2 * i + 1] = i + 1 < sn ? x[sn + i] + ((t[2 * i] + t[2 * i + 2]) >> 1) : x[sn + i] + t[2 * i];
+  } else {
+    const float* x = static_cast<const float*>(jb.plane) + (size_t)y * jb.stride;
+    float* t = static_cast<float*>(jb.tmp) + (size_t)y * jb.stride;
+    if (n == 1) {
+      if (lane == 0) t[0] = __fmul_rn(x[0], kRK);
+      return;
+    }
+    for (int i = lane; i < n; i += 32) {
+      const float v = i & 1 ? x[sn + (i >> 1)] : x[i >> 1];
+      t[i] = __fmul_rn(v, i & 1 ? kRInvK : kRK);
+    }
+    __syncwarp();
+    const float c[4] = {-kRDelta, -kRGamma, -kRBeta, -kRAlpha};
+    #pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      for (int j = (s & 1) + 2 * lane; j < n; j += 64)
+        t[j] = lifted(t[j], c[s], t[sym_at(j - 1, n)], t[sym_at(j + 1, n)]);
+      __syncwarp();
+    }
   }
-  const int sn = (n + 1) / 2;
-  for (int i = 0; i < n; ++i) {
-    const float v = i & 1 ? p[(size_t)(sn + (i >> 1)) * stride] : p[(size_t)(i >> 1) * stride];
-    t[(size_t)i * stride] = __fmul_rn(v, i & 1 ? kRInvK : kRK);
+}
+
+// Inverse 1-D transform of the columns of a job's tmp (low half of the rows
+// first) into its plane, interleaved. A CTA takes 32 columns x 64 output
+// rows and the 4 (9/7) or 2 (5/3) rows of halo each side in shared memory;
+// positions beyond the column's ends are loaded from their mirror images.
+// Whole-sample symmetric extension commutes with each lifting step (a
+// position and its mirror have the same parity and mirrored neighbours, and
+// l + r = r + l exactly), so every kept row equals the reference's value;
+// the 5/3 edge clamps are the same extension. The halo rows, whose outer
+// neighbours are missing, are not written.
+constexpr int kTileRows = kIdwtTileRows;
+__global__ void __launch_bounds__(256) idwt_cols_kernel(const IdwtJob* jobs, uint32_t njobs, uint32_t total_tiles) {
+  __shared__ float sh[(kTileRows + 8) * 33];
+  const uint32_t g = blockIdx.x;
+  if (g >= total_tiles) return;
+  const IdwtJob& jb = job_of(jobs, njobs, g, true);
+  const uint32_t tiles_x = (jb.rw + 31) / 32, t = g - jb.tile_base;
+  const int tx = (int)(t % tiles_x), ty = (int)(t / tiles_x);
+  const int lane = threadIdx.x & 31, ry = threadIdx.x >> 5;  // 8 row groups
+  const int x = tx * 32 + lane;
+  const bool col = x < (int)jb.rw;
+  const int n = (int)jb.rh, sn = (n + 1) / 2;
+  const size_t stride = jb.stride;
+  const int r0 = ty * kTileRows;
+  if (jb.reversible) {
+    const int32_t* src = static_cast<const int32_t*>(jb.tmp) + x;
+    int32_t* dst = static_cast<int32_t*>(jb.plane) + x;
+    int32_t* si = reinterpret_cast<int32_t*>(sh);
+    if (n == 1) {
+      if (ry == 0 && col) dst[0] = src[0];
+      return;
+    }
+    constexpr int halo = 2, m = kTileRows + 2 * halo;
+    for (int li = ry; li < m; li += 8) {
+      const int p = sym_at(r0 - halo + li, n);
+      si[li * 33 + lane] = col ? src[(size_t)(p & 1 ? sn + (p >> 1) : p >> 1) * stride] : 0;
+    }
+    __syncthreads();
+    for (int li = 1 + ry; li < m - 1; li += 8)  // even positions (r0 is even)
+      if (!(li & 1)) si[li * 33 + lane] -= (si[(li - 1) * 33 + lane] + si[(li + 1) * 33 + lane] + 2) >> 2;
+    __syncthreads();
+    for (int li = 1 + ry; li < m - 1; li += 8)
+      if (li & 1) si[li * 33 + lane] += (si[(li - 1) * 33 + lane] + si[(li + 1) * 33 + lane]) >> 1;
+    __syncthreads();
+    for (int li = halo + ry; li < halo + kTileRows; li += 8) {
+      const int i = r0 + li - halo;
+      if (col && i < n) dst[(size_t)i * stride] = si[li * 33 + lane];
+    }
+  } else {
+    const float* src = static_cast<const float*>(jb.tmp) + x;
+    float* dst = static_cast<float*>(jb.plane) + x;
+    if (n == 1) {
+      if (ry == 0 && col) dst[0] = __fmul_rn(src[0], kRK);
+      return;
+    }
+    constexpr int halo = 4, m = kTileRows + 2 * halo;
+    for (int li = ry; li < m; li += 8) {
+      const int p = sym_at(r0 - halo + li, n);
+      const float v = col ? src[(size_t)(p & 1 ? sn + (p >> 1) : p >> 1) * stride] : 0.0f;
+      sh[li * 33 + lane] = __fmul_rn(v, p & 1 ? kRInvK : kRK);
+    }
+    __syncthreads();
+    const float c[4] = {-kRDelta, -kRGamma, -kRBeta, -kRAlpha};
+    #pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      for (int li = 1 + ry; li < m - 1; li += 8)
+        if ((li & 1) == (s & 1))
+          sh[li * 33 + lane] = lifted(sh[li * 33 + lane], c[s], sh[(li - 1) * 33 + lane], sh[(li + 1) * 33 + lane]);
+      __syncthreads();
+    }
+    for (int li = halo + ry; li < halo + kTileRows; li += 8) {
+      const int i = r0 + li - halo;
+      if (col && i < n) dst[(size_t)i * stride] = sh[li * 33 + lane];
+    }
   }
-  const float c[4] = {-kRDelta, -kRGamma, -kRBeta, -kRAlpha};
-  #pragma unroll
-  for (int s = 0; s < 4; ++s)
-    for (int j = s & 1; j < n; j += 2)
-      t[(size_t)j * stride] =
-          lifted(t[(size_t)j * stride], c[s], t[(size_t)sym_at(j - 1, n) * stride], t[(size_t)sym_at(j + 1, n) * stride]);
-  for (int i = 0; i < n; ++i) p[(size_t)i * stride] = t[(size_t)i * stride];
 }
 
 __device__ __forceinline__ float clamp255(float v) { return fminf(fmaxf(v, 0.0f), 255.0f); }
@@ -200,107 +286,62 @@ __global__ void recon_ssim_kernel(ReconArgs r) {
 }
 
 // ------------------------------------------------------------- decoding --
-// Reconstruction of a decoded codestream (reconstruct, src/decode/
-// reconstruct.rs:24-304): the inverse 5/3 (src/dwt/rev53.rs:96-129 and
-// 419-497: per level rows then columns; even samples first,
-// s[i] - ((d[i-1] + d[i] + 2) >> 2) with the edges clamped, then odd samples
-// d[i] + ((e[i] + e[i+1]) >> 1), or d[i] + e[i] at the right edge) and
-// inverse RCT, or the inverse 9/7 above and inverse ICT; the level shift and
-// the 8-bit clamp (finalize, src/simd/scalar.rs:216-242).
-
-// Inverse 1-D 5/3 of row y: a warp per row, through the row's slice of tmp.
-__global__ void dec53_rows_kernel(int32_t* plane, int32_t* tmp, int stride, int rw, int rh) {
-  const int lane = threadIdx.x & 31;
-  const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (y >= rh || rw <= 1) return;
-  int32_t* x = plane + (size_t)y * stride;
-  int32_t* t = tmp + (size_t)y * stride;
-  const int sn = (rw + 1) / 2, dn = rw - sn;
-  for (int i = lane; i < sn; i += 32) {
-    const int l = min(max(i - 1, 0), dn - 1), r = min(i, dn - 1);
-    t[2 * i] = x[i] - ((x[sn + l] + x[sn + r] + 2) >> 2);
-  }
-  __syncwarp();
-  for (int i = lane; i < dn; i += 32)
-    t[2 * i + 1] = i + 1 < sn ? x[sn + i] + ((t[2 * i] + t[2 * i + 2]) >> 1) : x[sn + i] + t[2 * i];
-  __syncwarp();
-  for (int i = lane; i < rw; i += 32) x[i] = t[i];
-}
-
-// Inverse 1-D 5/3 of every column x < rw: a thread per column.
-__global__ void dec53_cols_kernel(int32_t* plane, int32_t* tmp, int stride, int rw, int rh) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= rw || rh <= 1) return;
-  int32_t* p = plane + x;
-  int32_t* t = tmp + x;
-  const size_t s = (size_t)stride;
-  const int sn = (rh + 1) / 2, dn = rh - sn;
-  for (int i = 0; i < sn; ++i) {
-    const int l = min(max(i - 1, 0), dn - 1), r = min(i, dn - 1);
-    t[2 * i * s] = p[i * s] - ((p[(sn + l) * s] + p[(sn + r) * s] + 2) >> 2);
-  }
-  for (int i = 0; i < dn; ++i)
-    t[(2 * i + 1) * s] =
-        i + 1 < sn ? p[(sn + i) * s] + ((t[2 * i * s] + t[(2 * i + 2) * s]) >> 1) : p[(sn + i) * s] + t[2 * i * s];
-  for (int i = 0; i < rh; ++i) p[i * s] = t[i * s];
-}
-
 __device__ __forceinline__ uint8_t clamp_int(int32_t v) { return (uint8_t)min(max(v + 128, 0), 255); }
 __device__ __forceinline__ uint8_t clamp_round(float v) {
   return (uint8_t)(int)fminf(fmaxf(roundf(__fadd_rn(v, 128.0f)), 0.0f), 255.0f);
 }
 
-// Inverse RCT (src/simd/scalar.rs:216-228) or ICT (scalar.rs:201-214) and
-// the interleaved 8-bit samples.
-__global__ void dec_pixels_kernel(DecodeArgs a) {
-  const size_t n = (size_t)a.width * a.height;
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (a.reversible) {
-    const int32_t* q = a.plane;
-    if (a.ncomp == 3 && a.mct) {
+// Inverse RCT (src/simd/scalar.rs:216-228) or ICT (scalar.rs:201-214), the
+// level shift and clamp (finalize, scalar.rs:230-242) of one sample of one
+// page, written interleaved.
+__global__ void dec_pixels_kernel(const PixJob* jobs, uint32_t njobs, uint64_t total) {
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total) return;
+  uint32_t lo = 0, hi = njobs;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (jobs[mid].pix_base <= g) lo = mid;
+    else hi = mid;
+  }
+  const PixJob& jb = jobs[lo];
+  const size_t n = jb.npx, i = g - jb.pix_base;
+  uint8_t* out = jb.px + (size_t)jb.ncomp * i;
+  if (jb.reversible) {
+    const int32_t* q = jb.planes;
+    if (jb.ncomp == 3 && jb.mct) {
       const int32_t yy = q[i], db = q[n + i], dr = q[2 * n + i];
-      const int32_t g = yy - ((db + dr) >> 2);
-      a.px[3 * i] = clamp_int(dr + g);
-      a.px[3 * i + 1] = clamp_int(g);
-      a.px[3 * i + 2] = clamp_int(db + g);
+      const int32_t gg = yy - ((db + dr) >> 2);
+      out[0] = clamp_int(dr + gg);
+      out[1] = clamp_int(gg);
+      out[2] = clamp_int(db + gg);
     } else {
-      for (int c = 0; c < a.ncomp; ++c) a.px[a.ncomp * i + c] = clamp_int(q[c * n + i]);
+      for (uint32_t c = 0; c < jb.ncomp; ++c) out[c] = clamp_int(q[c * n + i]);
     }
   } else {
-    const float* f = reinterpret_cast<const float*>(a.plane);
-    if (a.ncomp == 3 && a.mct) {
+    const float* f = reinterpret_cast<const float*>(jb.planes);
+    if (jb.ncomp == 3 && jb.mct) {
       const float yy = f[i], cb = f[n + i], cr = f[2 * n + i];
-      a.px[3 * i] = clamp_round(__fadd_rn(yy, __fmul_rn(1.402f, cr)));
-      a.px[3 * i + 1] = clamp_round(__fadd_rn(__fadd_rn(yy, -__fmul_rn(0.34413f, cb)), -__fmul_rn(0.71414f, cr)));
-      a.px[3 * i + 2] = clamp_round(__fadd_rn(yy, __fmul_rn(1.772f, cb)));
+      out[0] = clamp_round(__fadd_rn(yy, __fmul_rn(1.402f, cr)));
+      out[1] = clamp_round(__fadd_rn(__fadd_rn(yy, -__fmul_rn(0.34413f, cb)), -__fmul_rn(0.71414f, cr)));
+      out[2] = clamp_round(__fadd_rn(yy, __fmul_rn(1.772f, cb)));
     } else {
-      for (int c = 0; c < a.ncomp; ++c) a.px[a.ncomp * i + c] = clamp_round(f[c * n + i]);
+      for (uint32_t c = 0; c < jb.ncomp; ++c) out[c] = clamp_round(f[c * n + i]);
     }
   }
 }
 
 }  // namespace
 
-void launch_decode_reconstruct(const DecodeArgs& a, const std::pair<int, int>* ladder, int levels, cudaStream_t st) {
-  const size_t n = (size_t)a.width * a.height;
-  for (int c = 0; c < a.ncomp; ++c)
-    for (int l = 1; l <= levels; ++l) {
-      const int rw = ladder[l].first, rh = ladder[l].second;
-      if (rw == 0 || rh == 0) continue;
-      const unsigned rows_grid = (unsigned)(((size_t)rh * 32 + 255) / 256), cols_grid = (unsigned)((rw + 127) / 128);
-      if (a.reversible) {
-        int32_t* plane = a.plane + (size_t)c * n;
-        dec53_rows_kernel<<<rows_grid, 256, 0, st>>>(plane, a.tmp, (int)a.width, rw, rh);
-        dec53_cols_kernel<<<cols_grid, 128, 0, st>>>(plane, a.tmp, (int)a.width, rw, rh);
-      } else {
-        float* plane = reinterpret_cast<float*>(a.plane) + (size_t)c * n;
-        float* tmp = reinterpret_cast<float*>(a.tmp);
-        recon_rows_kernel<<<rows_grid, 256, 0, st>>>(plane, tmp, (int)a.width, rw, rh);
-        recon_cols_kernel<<<cols_grid, 128, 0, st>>>(plane, tmp, (int)a.width, rw, rh);
-      }
-    }
-  dec_pixels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
+void launch_idwt_level(const IdwtJob* jobs, uint32_t njobs, uint32_t total_rows, uint32_t total_tiles,
+                       cudaStream_t st) {
+  if (njobs == 0) return;
+  if (total_rows) idwt_rows_kernel<<<(unsigned)(((size_t)total_rows * 32 + 255) / 256), 256, 0, st>>>(jobs, njobs, total_rows);
+  if (total_tiles) idwt_cols_kernel<<<total_tiles, 256, 0, st>>>(jobs, njobs, total_tiles);
+}
+
+void launch_dec_pixels(const PixJob* jobs, uint32_t njobs, uint64_t total_px, cudaStream_t st) {
+  if (njobs == 0 || total_px == 0) return;
+  dec_pixels_kernel<<<(unsigned)((total_px + 255) / 256), 256, 0, st>>>(jobs, njobs, total_px);
 }
 
 void launch_recon(const ReconArgs& r, const std::pair<int, int>* ladder, int levels, cudaStream_t st) {
@@ -308,15 +349,31 @@ void launch_recon(const ReconArgs& r, const std::pair<int, int>* ladder, int lev
   cudaMemsetAsync(r.plane, 0, n * r.ncomp * sizeof(float), st);
   cudaMemsetAsync(r.stats, 0, 2 * sizeof(double), st);
   if (r.nblocks) recon_dequant_kernel<<<(unsigned)(((size_t)r.nblocks * 32 + 255) / 256), 256, 0, st>>>(r);
-  for (int c = 0; c < r.ncomp; ++c) {
-    float* plane = r.plane + (size_t)c * n;
-    for (int l = 1; l <= levels; ++l) {
-      const int rw = ladder[l].first, rh = ladder[l].second;
-      if (rw == 0 || rh == 0) continue;
-      recon_rows_kernel<<<(unsigned)(((size_t)rh * 32 + 255) / 256), 256, 0, st>>>(plane, r.tmp, (int)r.width, rw, rh);
-      recon_cols_kernel<<<(unsigned)((rw + 127) / 128), 128, 0, st>>>(plane, r.tmp, (int)r.width, rw, rh);
+  // every component of a level in one launch, each with its own tmp plane
+  std::vector<IdwtJob> jobs;
+  std::vector<uint32_t> first(levels + 2, 0), rows(levels + 2, 0), tiles(levels + 2, 0);
+  for (int l = 1; l <= levels; ++l) {
+    first[l] = (uint32_t)jobs.size();
+    const uint32_t rw = (uint32_t)ladder[l].first, rh = (uint32_t)ladder[l].second;
+    for (int c = 0; c < r.ncomp && rw && rh; ++c) {
+      IdwtJob j{};
+      j.plane = r.plane + (size_t)c * n;
+      j.tmp = r.tmp + (size_t)c * n;
+      j.stride = r.width;
+      j.rw = rw;
+      j.rh = rh;
+      j.reversible = 0;
+      j.row_base = rows[l];
+      j.tile_base = tiles[l];
+      rows[l] += rh;
+      tiles[l] += ((rw + 31) / 32) * ((rh + kIdwtTileRows - 1) / kIdwtTileRows);
+      jobs.push_back(j);
     }
   }
+  first[levels + 1] = (uint32_t)jobs.size();
+  if (!jobs.empty()) cudaMemcpyAsync(r.jobs, jobs.data(), jobs.size() * sizeof(IdwtJob), cudaMemcpyHostToDevice, st);
+  for (int l = 1; l <= levels; ++l)
+    launch_idwt_level(r.jobs + first[l], first[l + 1] - first[l], rows[l], tiles[l], st);
   recon_pixels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(r);
   const int nb8 = (int)(r.width / 8) * (int)(r.height / 8);
   if (nb8 > 0) recon_ssim_kernel<<<(unsigned)((nb8 + 255) / 256), 256, 0, st>>>(r);

@@ -1,17 +1,27 @@
 // Tier-1 decoding on the device: the MQ decoder and the three decoding
-// passes of every code-block (decode_tile_components / the block decoder of
-// src/decode/t1.rs:87-210, MqDecoder of src/mq/mod.rs, the context rules of
-// src/tier1/*).
+// passes of every code-block (decode_codeblock, src/decode/t1.rs:87-210;
+// the MQ decoder of src/mq/mod.rs; the context rules of src/tier1/*).
 //
 // Decoding is sequential within a code-block (every decoded bit changes the
-// contexts of the samples after it), so one lane of a warp decodes one
-// block, its significance, visited, refined and sign states held as 64-bit
-// row masks in shared memory (a row per mask and row, zero rows above and
-// below), from which a sample's neighbourhood is a few shifts. The decoded
-// magnitudes accumulate in the component plane; at the end the whole warp
-// writes the block's signed coefficients (reversible codestreams) or their
-// midpoint dequantised values (irreversible: sign * (|q| + 0.5) * step,
-// src/simd/scalar.rs:122-129) in place.
+// contexts of the samples after it), so one lane of a warp runs a block's
+// decoder while the warp's other lanes wait; a CTA holds 8 such warps.
+//  - State: significance, sign, visited and refined flags as 64-bit row
+//    masks in shared memory (a row per mask, zero rows above and below).
+//    A stripe's rows (4, plus the rows above and below for significance and
+//    sign) are held in registers while the stripe is coded, so a sample's
+//    neighbourhood is a few shifts.
+//  - Skipping: each pass visits only the columns of a stripe that can hold
+//    a decision: significance propagation the columns with an insignificant
+//    sample next to a significant one (recomputed when a decision makes a
+//    sample significant), refinement the columns with a significant
+//    unvisited sample, cleanup the columns with an unvisited insignificant
+//    one. Samples are still decided in the standard's scan order.
+//  - Magnitudes: the decoded bits of a bit-plane are gathered as row masks;
+//    after each bit-plane the whole warp ORs them into the component plane
+//    (lane l owns columns l and l + 32). At the end it writes the block's
+//    signed coefficients (reversible codestreams) or their midpoint
+//    dequantised values (irreversible: sign * (|q| + 0.5) * step,
+//    src/simd/scalar.rs:122-129) in place.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -23,7 +33,7 @@ namespace jp2g {
 
 namespace {
 
-constexpr int kDecWarps = 4;
+constexpr int kDecWarps = 8;
 constexpr int kCtxZC0 = 0, kCtxMR = 14, kCtxAGG = 17, kCtxUNI = 18;
 
 struct DecTables {
@@ -34,8 +44,9 @@ struct DecTables {
 };
 __constant__ DecTables c_dec;
 
-struct BlockState {
-  uint64_t sig[66], vis[66], ref[66], sgn[66];  // row y at y + 1
+struct WarpState {
+  uint64_t sig[66], sgn[66], vis[66], ref[66];  // row y at y + 1
+  uint64_t bits[64];                             // the current bit-plane's decoded 1 bits
   uint8_t ctx[20];
 };
 
@@ -45,6 +56,7 @@ struct MqDecoder {
   const uint8_t* b;
   uint32_t n, bp;
   uint32_t a, c, ct;
+  uint8_t* ctx;
   __device__ uint32_t at(uint32_t i) const { return i < n ? b[i] : 0xffu; }
   __device__ void bytein() {
     const uint32_t next = at(bp + 1);
@@ -63,10 +75,11 @@ struct MqDecoder {
       ct = 8;
     }
   }
-  __device__ void init(const uint8_t* data, uint32_t len) {
+  __device__ void init(const uint8_t* data, uint32_t len, uint8_t* contexts) {
     b = data;
     n = len;
     bp = 0;
+    ctx = contexts;
     c = n == 0 ? (0xffu << 16) : ((uint32_t)b[0] << 16);
     ct = 0;
     bytein();
@@ -74,41 +87,32 @@ struct MqDecoder {
     ct = ct >= 7 ? ct - 7 : 0;
     a = 0x8000u;
   }
-  __device__ uint32_t decode(uint8_t* ctx, int cx) {
+  __device__ __forceinline__ uint32_t decode(int cx) {
     const uint32_t st = ctx[cx], e = c_dec.mq[st];
     const uint32_t qe = e & 0xffffu, mps = st & 1u;
     uint32_t bit;
     a -= qe;
     if ((c >> 16) < qe) {
-      const uint32_t post = a;
+      const bool mps_path = a < qe;
       a = qe;
-      if (post < qe) {
-        ctx[cx] = (uint8_t)((e >> 16) & 0xffu);
-        bit = mps;
-      } else {
-        ctx[cx] = (uint8_t)(e >> 24);
-        bit = mps ^ 1u;
-      }
+      ctx[cx] = (uint8_t)(mps_path ? (e >> 16) & 0xffu : e >> 24);
+      bit = mps_path ? mps : mps ^ 1u;
     } else {
       c -= qe << 16;
       if ((a & 0x8000u) == 0) {
-        if (a < qe) {
-          ctx[cx] = (uint8_t)(e >> 24);
-          bit = mps ^ 1u;
-        } else {
-          ctx[cx] = (uint8_t)((e >> 16) & 0xffu);
-          bit = mps;
-        }
+        const bool lps_path = a < qe;
+        ctx[cx] = (uint8_t)(lps_path ? e >> 24 : (e >> 16) & 0xffu);
+        bit = lps_path ? mps ^ 1u : mps;
       } else {
-        bit = mps;
+        return mps;
       }
     }
-    while (a < 0x8000u) {
+    do {
       if (ct == 0) bytein();
       a <<= 1;
       c <<= 1;
       --ct;
-    }
+    } while (a < 0x8000u);
     return bit;
   }
 };
@@ -117,158 +121,272 @@ struct MqDecoder {
 __device__ __forceinline__ uint32_t win3(uint64_t row, int x) {
   return (uint32_t)(x == 0 ? row << 1 : row >> (x - 1)) & 7u;
 }
+__device__ __forceinline__ uint64_t spread(uint64_t m) { return m | (m << 1) | (m >> 1); }
+__device__ __forceinline__ uint64_t above(int x) { return x >= 63 ? 0ull : ~0ull << (x + 1); }
+
+// One stripe's state while it is coded: S/G rows k-1 .. k+4, V/R rows k .. k+3,
+// B the stripe's decoded 1 bits of the current bit-plane.
+struct Stripe {
+  uint64_t S[6], G[6], V[4], R[4], B[4];
+};
 
 struct BlockDecoder {
-  BlockState& s;
+  WarpState& s;
   MqDecoder mq;
-  int w, h;
   const uint8_t* zc;
-  int32_t* plane;  // the block's first sample; rows `stride` apart
-  uint32_t stride;
+  uint64_t wmask;
 
-  // Neighbour-significance index (bit 0 NW, 1 N, 2 NE, 3 W, 5 E, 6 SW, 7 S,
-  // 8 SE) of sample (x, y) in the current state.
-  __device__ uint32_t nmask(int x, int y) const {
-    const uint32_t up = win3(s.sig[y], x), mid = win3(s.sig[y + 1], x), dn = win3(s.sig[y + 2], x);
+  __device__ void load(int k, Stripe& t) const {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      t.S[i] = s.sig[k + i];
+      t.G[i] = s.sgn[k + i];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      t.V[i] = s.vis[k + 1 + i];
+      t.R[i] = s.ref[k + 1 + i];
+      t.B[i] = 0;
+    }
+  }
+  __device__ void store(int k, const Stripe& t) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      s.sig[k + 1 + i] = t.S[i + 1];
+      s.sgn[k + 1 + i] = t.G[i + 1];
+      s.vis[k + 1 + i] = t.V[i];
+      s.ref[k + 1 + i] = t.R[i];
+      s.bits[k + i] |= t.B[i];
+    }
+  }
+
+  // Neighbour-significance index of (x, k + r) (bit 0 NW, 1 N, 2 NE, 3 W,
+  // 5 E, 6 SW, 7 S, 8 SE; src/tier1/consts.rs).
+  template <int r>
+  __device__ __forceinline__ uint32_t nmask(const Stripe& t, int x) const {
+    const uint32_t up = win3(t.S[r], x), mid = win3(t.S[r + 1], x), dn = win3(t.S[r + 2], x);
     return up | ((mid & 1u) << 3) | ((mid & 4u) << 3) | (dn << 6);
   }
-  __device__ bool bit_at(const uint64_t* m, int x, int y) const { return (m[y + 1] >> x) & 1u; }
-  __device__ void set(uint64_t* m, int x, int y) { m[y + 1] |= 1ull << x; }
-  __device__ void clear(uint64_t* m, int x, int y) { m[y + 1] &= ~(1ull << x); }
-  __device__ void add_magnitude(int x, int y, uint32_t one) { plane[(size_t)y * stride + x] |= (int32_t)one; }
 
   // Sign of a newly significant sample (src/tier1/helpers.rs:52-88).
-  __device__ void decode_sign(int x, int y) {
-    const uint32_t ws = x > 0 && bit_at(s.sig, x - 1, y), wg = x > 0 && bit_at(s.sgn, x - 1, y);
-    const uint32_t es = x + 1 < w && bit_at(s.sig, x + 1, y), eg = x + 1 < w && bit_at(s.sgn, x + 1, y);
-    const uint32_t ns = (s.sig[y] >> x) & 1u, ng = (s.sgn[y] >> x) & 1u;
-    const uint32_t ss = (s.sig[y + 2] >> x) & 1u, sg = (s.sgn[y + 2] >> x) & 1u;
+  template <int r>
+  __device__ __forceinline__ void sign(Stripe& t, int x) {
+    const uint64_t bx = 1ull << x;
+    const uint32_t ws = x > 0 ? (uint32_t)(t.S[r + 1] >> (x - 1)) & 1u : 0u;
+    const uint32_t wg = x > 0 ? (uint32_t)(t.G[r + 1] >> (x - 1)) & 1u : 0u;
+    const uint32_t es = x < 63 ? (uint32_t)(t.S[r + 1] >> (x + 1)) & 1u : 0u;
+    const uint32_t eg = x < 63 ? (uint32_t)(t.G[r + 1] >> (x + 1)) & 1u : 0u;
+    const uint32_t ns = (uint32_t)(t.S[r] >> x) & 1u, ng = (uint32_t)(t.G[r] >> x) & 1u;
+    const uint32_t ss = (uint32_t)(t.S[r + 2] >> x) & 1u, sg = (uint32_t)(t.G[r + 2] >> x) & 1u;
     const uint32_t lu = (ws << 3) | (ws & wg) | (ns << 1) | ((ns & ng) << 4) | (es << 5) | ((es & eg) << 2) |
                         (ss << 7) | ((ss & sg) << 6);
-    const uint32_t sign = mq.decode(s.ctx, c_dec.sc[lu]) ^ c_dec.spb[lu];
-    set(s.sig, x, y);
-    if (sign) set(s.sgn, x, y);
+    const uint32_t neg = mq.decode(c_dec.sc[lu]) ^ c_dec.spb[lu];
+    t.S[r + 1] |= bx;
+    if (neg) t.G[r + 1] |= bx;
   }
 
-  __device__ void sigpass_step(int x, int y, uint32_t one) {
-    if (bit_at(s.sig, x, y)) return;
-    const uint32_t nm = nmask(x, y);
-    if (nm == 0) return;
-    const uint32_t bit = mq.decode(s.ctx, zc[nm]);
-    set(s.vis, x, y);
-    if (bit) {
-      add_magnitude(x, y, one);
-      decode_sign(x, y);
-    }
-  }
-  __device__ void refpass_step(int x, int y, uint32_t one) {
-    if (!bit_at(s.sig, x, y) || bit_at(s.vis, x, y)) return;
-    const int cx = bit_at(s.ref, x, y) ? kCtxMR + 2 : (nmask(x, y) ? kCtxMR + 1 : kCtxMR);
-    if (mq.decode(s.ctx, cx)) add_magnitude(x, y, one);
-    set(s.ref, x, y);
-  }
-  __device__ void cleanup_step(int x, int y, uint32_t one) {
-    if (bit_at(s.sig, x, y) || bit_at(s.vis, x, y)) {
-      clear(s.vis, x, y);
-      return;
-    }
-    const uint32_t nm = nmask(x, y);
-    const uint32_t bit = mq.decode(s.ctx, nm ? zc[nm] : kCtxZC0);
-    clear(s.vis, x, y);
-    if (bit) {
-      add_magnitude(x, y, one);
-      decode_sign(x, y);
-    }
-  }
-  // A full stripe's column with nothing significant or visited in it or
-  // around it codes as a run (src/tier1/flags.rs:219-235).
-  __device__ bool clean(int x, int k) const {
+  // Columns of the stripe with an insignificant sample next to a
+  // significant one.
+  __device__ __forceinline__ uint64_t sig_candidates(const Stripe& t, int lim) const {
+    uint64_t m = 0;
+#pragma unroll
     for (int r = 0; r < 4; ++r)
-      if (bit_at(s.sig, x, k + r) || bit_at(s.vis, x, k + r) || nmask(x, k + r)) return false;
+      if (r < lim) m |= ~t.S[r + 1] & (spread(t.S[r]) | spread(t.S[r + 2]) | (t.S[r + 1] << 1) | (t.S[r + 1] >> 1));
+    return m & wmask;
+  }
+
+  template <int r>
+  __device__ __forceinline__ bool sig_one(Stripe& t, int x, uint64_t bx) {
+    if (t.S[r + 1] & bx) return false;
+    const uint32_t nm = nmask<r>(t, x);
+    if (!nm) return false;
+    const uint32_t bit = mq.decode(zc[nm]);
+    t.V[r] |= bx;
+    if (!bit) return false;
+    t.B[r] |= bx;
+    sign<r>(t, x);
     return true;
   }
 
-  __device__ void sigpass(int bp) {
-    const uint32_t one = 1u << bp;
-    for (int k = 0; k < h; k += 4) {
-      const int lim = min(4, h - k);
-      for (int x = 0; x < w; ++x)
-        for (int r = 0; r < lim; ++r) sigpass_step(x, k + r, one);
+  __device__ void sigpass(int k, int lim) {
+    Stripe t;
+    load(k, t);
+    uint64_t cols = sig_candidates(t, lim);
+    while (cols) {
+      const int x = __ffsll((long long)cols) - 1;
+      const uint64_t bx = 1ull << x;
+      bool grew = sig_one<0>(t, x, bx);
+      if (lim > 1) grew |= sig_one<1>(t, x, bx);
+      if (lim > 2) grew |= sig_one<2>(t, x, bx);
+      if (lim > 3) grew |= sig_one<3>(t, x, bx);
+      cols &= above(x);
+      if (grew) cols = sig_candidates(t, lim) & above(x);
+    }
+    store(k, t);
+  }
+
+  template <int r>
+  __device__ __forceinline__ void ref_one(Stripe& t, int x, uint64_t bx) {
+    if (!(t.S[r + 1] & ~t.V[r] & bx)) return;
+    const int cx = (t.R[r] & bx) ? kCtxMR + 2 : (nmask<r>(t, x) ? kCtxMR + 1 : kCtxMR);
+    if (mq.decode(cx)) t.B[r] |= bx;
+    t.R[r] |= bx;
+  }
+
+  __device__ void refpass(int k, int lim) {
+    Stripe t;
+    load(k, t);
+    uint64_t cols = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      if (r < lim) cols |= t.S[r + 1] & ~t.V[r];
+    cols &= wmask;
+    while (cols) {
+      const int x = __ffsll((long long)cols) - 1;
+      const uint64_t bx = 1ull << x;
+      ref_one<0>(t, x, bx);
+      if (lim > 1) ref_one<1>(t, x, bx);
+      if (lim > 2) ref_one<2>(t, x, bx);
+      if (lim > 3) ref_one<3>(t, x, bx);
+      cols &= above(x);
+    }
+    store(k, t);
+  }
+
+  template <int r>
+  __device__ __forceinline__ void cleanup_one(Stripe& t, int x, uint64_t bx) {
+    if ((t.S[r + 1] | t.V[r]) & bx) return;
+    const uint32_t nm = nmask<r>(t, x);
+    if (mq.decode(nm ? zc[nm] : kCtxZC0)) {
+      t.B[r] |= bx;
+      sign<r>(t, x);
     }
   }
-  __device__ void refpass(int bp) {
-    const uint32_t one = 1u << bp;
-    for (int k = 0; k < h; k += 4) {
-      const int lim = min(4, h - k);
-      for (int x = 0; x < w; ++x)
-        for (int r = 0; r < lim; ++r) refpass_step(x, k + r, one);
-    }
-  }
-  __device__ void cleanup(int bp) {
-    const uint32_t one = 1u << bp;
-    for (int k = 0; k < h; k += 4) {
-      const int lim = min(4, h - k);
-      for (int x = 0; x < w; ++x) {
-        if (lim == 4 && clean(x, k)) {
-          if (mq.decode(s.ctx, kCtxAGG) == 0) continue;
-          int rl = (int)mq.decode(s.ctx, kCtxUNI) << 1;
-          rl |= (int)mq.decode(s.ctx, kCtxUNI);
-          add_magnitude(x, k + rl, one);
-          decode_sign(x, k + rl);
-          clear(s.vis, x, k + rl);
-          for (int r = rl + 1; r < 4; ++r) cleanup_step(x, k + r, one);
+
+  __device__ void cleanup(int k, int lim) {
+    Stripe t;
+    load(k, t);
+    uint64_t busy = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      if (r < lim) busy |= t.S[r + 1] | t.V[r];
+    uint64_t cols = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      if (r < lim) cols |= ~(t.S[r + 1] | t.V[r]);
+    cols &= wmask;
+    while (cols) {
+      const int x = __ffsll((long long)cols) - 1;
+      const uint64_t bx = 1ull << x;
+      cols &= above(x);
+      // a full stripe's column with nothing significant or visited in it or
+      // around it is coded as a run (src/tier1/flags.rs:219-235)
+      if (lim == 4 && !(busy & bx) && win3(t.S[0] | t.S[1] | t.S[2] | t.S[3] | t.S[4] | t.S[5], x) == 0) {
+        if (mq.decode(kCtxAGG) == 0) continue;
+        int rl = (int)mq.decode(kCtxUNI) << 1;
+        rl |= (int)mq.decode(kCtxUNI);
+        if (rl == 0) {
+          t.B[0] |= bx;
+          sign<0>(t, x);
+          cleanup_one<1>(t, x, bx);
+          cleanup_one<2>(t, x, bx);
+          cleanup_one<3>(t, x, bx);
+        } else if (rl == 1) {
+          t.B[1] |= bx;
+          sign<1>(t, x);
+          cleanup_one<2>(t, x, bx);
+          cleanup_one<3>(t, x, bx);
+        } else if (rl == 2) {
+          t.B[2] |= bx;
+          sign<2>(t, x);
+          cleanup_one<3>(t, x, bx);
         } else {
-          for (int r = 0; r < lim; ++r) cleanup_step(x, k + r, one);
+          t.B[3] |= bx;
+          sign<3>(t, x);
         }
+      } else {
+        cleanup_one<0>(t, x, bx);
+        if (lim > 1) cleanup_one<1>(t, x, bx);
+        if (lim > 2) cleanup_one<2>(t, x, bx);
+        if (lim > 3) cleanup_one<3>(t, x, bx);
       }
     }
-    for (int y = 0; y < h; ++y) s.vis[y + 1] = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) t.V[r] = 0;
+    store(k, t);
   }
 };
 
-__global__ void __launch_bounds__(kDecWarps * 32) t1_decode_kernel(DecodeArgs a) {
-  __shared__ BlockState st_all[kDecWarps];
+__global__ void __launch_bounds__(kDecWarps * 32) t1_decode_kernel(const DecBlock* blocks, uint32_t nblocks,
+                                                                     const uint8_t* data, int32_t* planes) {
+  __shared__ WarpState st_all[kDecWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t blk = blockIdx.x * kDecWarps + wid;
-  if (blk >= a.nblocks) return;
-  BlockState& s = st_all[wid];
-  const DecBlock d = a.blocks[blk];
-  for (int i = lane; i < 66; i += 32) s.sig[i] = s.vis[i] = s.ref[i] = s.sgn[i] = 0;
-  int32_t* plane = a.plane + (size_t)d.comp * a.width * a.height + (size_t)d.y0 * a.width + d.x0;
+  if (blk >= nblocks) return;
+  WarpState& s = st_all[wid];
+  const DecBlock d = blocks[blk];
+  for (int i = lane; i < 66; i += 32) s.sig[i] = s.sgn[i] = s.vis[i] = s.ref[i] = 0;
+  for (int i = lane; i < 64; i += 32) s.bits[i] = 0;
+  // initial context states (src/mq/mod.rs:195-200)
+  if (lane < 20) s.ctx[lane] = lane == kCtxUNI ? 92 : lane == kCtxAGG ? 6 : lane == kCtxZC0 ? 8 : 0;
+  int32_t* plane = planes + d.plane_off;
+  const int w = d.w, h = d.h;
+  const int x0 = lane, x1 = lane + 32;
   __syncwarp();
-  if (lane == 0 && d.npasses > 0) {
-    for (int i = 0; i < 20; ++i) s.ctx[i] = 0;
-    s.ctx[kCtxUNI] = 92;  // src/mq/mod.rs:195-200
-    s.ctx[kCtxAGG] = 6;
-    s.ctx[kCtxZC0] = 8;
-    BlockDecoder dec{s, {}, d.w, d.h, c_dec.zc + (d.orient & 3) * 512, plane, a.width};
-    dec.mq.init(a.data + d.data_off, d.data_len);
-    const int top = (int)d.mb - (int)d.zbp - 1;  // checked on the host: 0..30
-    int remaining = d.npasses;
-    dec.cleanup(top);
-    --remaining;
-    for (int bp = top - 1; bp >= 0 && remaining > 0; --bp) {
-      dec.sigpass(bp);
-      if (--remaining == 0) break;
-      dec.refpass(bp);
-      if (--remaining == 0) break;
-      dec.cleanup(bp);
-      --remaining;
-    }
-  }
-  __syncwarp();
-  // signed coefficients, or their midpoint dequantised values
-  for (int i = lane; i < d.w * d.h; i += 32) {
-    const int y = i / d.w, x = i - y * d.w;
-    int32_t* p = plane + (size_t)y * a.width + x;
-    const int32_t m = *p;
-    const bool neg = (s.sgn[y + 1] >> x) & 1u;
-    if (a.reversible) {
-      *p = neg ? -m : m;
+  BlockDecoder dec{s, {}, c_dec.zc + (d.orient & 3) * 512, w == 64 ? ~0ull : (1ull << w) - 1};
+  if (lane == 0 && d.npasses > 0) dec.mq.init(data + d.data_off, d.data_len, s.ctx);
+  // pass sequence: cleanup of the top bit-plane, then significance,
+  // refinement and cleanup per bit-plane until the block's passes end
+  const int top = (int)d.mb - (int)d.zbp - 1;  // checked on the host: 0..30
+  int remaining = d.npasses;
+  for (int bp = top; bp >= 0 && remaining > 0; --bp) {
+    if (lane == 0) {
+      if (bp < top) {
+        for (int k = 0; k < h; k += 4) dec.sigpass(k, min(4, h - k));
+        if (--remaining > 0) {
+          for (int k = 0; k < h; k += 4) dec.refpass(k, min(4, h - k));
+          if (--remaining > 0) {
+            for (int k = 0; k < h; k += 4) dec.cleanup(k, min(4, h - k));
+            --remaining;
+          }
+        }
+      } else {
+        for (int k = 0; k < h; k += 4) dec.cleanup(k, min(4, h - k));
+        --remaining;
+      }
     } else {
-      float v = 0.0f;
-      if (m != 0) v = __fmul_rn(__fmul_rn(neg ? -1.0f : 1.0f, __fadd_rn((float)(uint32_t)m, 0.5f)), d.step);
-      *p = __float_as_int(v);
+      remaining -= bp < top ? min(3, remaining) : 1;
+    }
+    __syncwarp();
+    const int32_t one = (int32_t)(1u << bp);
+    for (int y = 0; y < h; ++y) {
+      const uint64_t b = s.bits[y];
+      if (!b) continue;
+      int32_t* row = plane + (size_t)y * d.stride;
+      if (x0 < w && ((b >> x0) & 1u)) row[x0] |= one;
+      if (x1 < w && ((b >> x1) & 1u)) row[x1] |= one;
+    }
+    __syncwarp();
+    for (int i = lane; i < 64; i += 32) s.bits[i] = 0;
+    __syncwarp();
+  }
+  // signed coefficients, or their midpoint dequantised values
+  for (int y = 0; y < h; ++y) {
+    const uint64_t neg = s.sgn[y + 1];
+    int32_t* row = plane + (size_t)y * d.stride;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int x = j ? x1 : x0;
+      if (x >= w) continue;
+      const int32_t m = row[x];
+      const bool n = (neg >> x) & 1u;
+      if (d.reversible) {
+        row[x] = n ? -m : m;
+      } else {
+        float v = 0.0f;
+        if (m != 0) v = __fmul_rn(__fmul_rn(n ? -1.0f : 1.0f, __fadd_rn((float)(uint32_t)m, 0.5f)), d.step);
+        row[x] = __float_as_int(v);
+      }
     }
   }
 }
@@ -284,9 +402,10 @@ bool upload_decode_tables(const uint8_t* zc, const uint8_t* sc, const uint8_t* s
   return cudaMemcpyToSymbol(c_dec, &t, sizeof t) == cudaSuccess;
 }
 
-void launch_t1_decode(const DecodeArgs& a, cudaStream_t st) {
-  if (a.nblocks == 0) return;
-  t1_decode_kernel<<<(a.nblocks + kDecWarps - 1) / kDecWarps, kDecWarps * 32, 0, st>>>(a);
+void launch_t1_decode(const DecBlock* blocks, uint32_t nblocks, const uint8_t* data, int32_t* planes,
+                      cudaStream_t st) {
+  if (nblocks == 0) return;
+  t1_decode_kernel<<<(nblocks + kDecWarps - 1) / kDecWarps, kDecWarps * 32, 0, st>>>(blocks, nblocks, data, planes);
 }
 
 }  // namespace jp2g

@@ -184,7 +184,8 @@ struct Decoded {
   int ncomp;
   Planes comps;
 };
-Decoded decode(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane = false);
+Decoded decode(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane = false,
+               bool accept_empty_segments = false);
 
 // Quality metrics as encode_with_psnr defines them.
 void quality_metrics(const Plan& p, const Planes& px, const EncodeOptions& opt,

@@ -303,10 +303,12 @@ int orc_block_summary(const uint8_t* px, uint32_t w, uint32_t h, int ncomp,
 // Decode J2K/JP2 bytes -> interleaved 8-bit pixels (caller buffer W*H*C).
 // The same, optionally reading RCT chroma code-blocks with the extra
 // bit-plane their encoder used (the reference's decoder does not).
-int orc_decode_ex(const uint8_t* bytes, size_t n, int rct_chroma_extra_bitplane, uint32_t* w, uint32_t* h,
+// flags: bit 0 = the extra RCT chroma bit-plane, bit 1 = accept code-blocks
+// whose segment has zero bytes.
+int orc_decode_ex(const uint8_t* bytes, size_t n, int flags, uint32_t* w, uint32_t* h,
                   int* ncomp, uint8_t* px, size_t cap) {
   try {
-    orc::Decoded d = orc::decode(bytes, n, rct_chroma_extra_bitplane != 0);
+    orc::Decoded d = orc::decode(bytes, n, (flags & 1) != 0, (flags & 2) != 0);
     *w = d.width;
     *h = d.height;
     *ncomp = d.ncomp;

@@ -15,7 +15,7 @@
 namespace orc {
 
 std::vector<int32_t> decode_block(const uint8_t* data, size_t n, int w, int h,
-                                  Band band, int mb, int zbp, int npasses);
+                                  Band band, int mb, int zbp, int npasses, bool allow_empty = false);
 
 template <class F>
 static void par_for(int n, int threads, F&& f) {
@@ -735,7 +735,7 @@ struct DTagTree {
 };
 }  // namespace
 
-Decoded decode(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane) {
+Decoded decode(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane, bool accept_empty_segments) {
 
   const uint8_t* cs = bytes;
   size_t csn = n;
@@ -870,7 +870,7 @@ Decoded decode(const uint8_t* bytes, size_t n, bool rct_chroma_extra_bitplane) {
         // at q >= 100 (backend.rs:179-189), which QCD does not signal
         int mb = guard - 1 + steps[si].first + (rct_chroma_extra_bitplane && rev && mct && comp > 0 ? 1 : 0);
         int bw = b.x1 - b.x0, bh = b.y1 - b.y0;
-        auto dv = decode_block(cs + body, b.len, bw, bh, rc.band, mb, b.zbp, b.np);
+        auto dv = decode_block(cs + body, b.len, bw, bh, rc.band, mb, b.zbp, b.np, accept_empty_segments);
         for (int y = 0; y < bh; ++y)
           for (int x = 0; x < bw; ++x) coef[comp][(size_t)(b.y0 + y) * W + b.x0 + x] = dv[(size_t)y * bw + x];
         body += b.len;

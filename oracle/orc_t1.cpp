@@ -604,14 +604,16 @@ EncBlock encode_block(const int32_t* coefs, int w, int h, Band band, int mb) {
 // ------------------------------------------------------- Tier-1 decoding ---
 // Code-block decoder used for round trips (src/decode/t1.rs:87-400).
 std::vector<int32_t> decode_block(const uint8_t* data, size_t n, int w, int h,
-                                  Band band, int mb, int zbp, int npasses);
+                                  Band band, int mb, int zbp, int npasses, bool allow_empty = false);
 
+// allow_empty: a segment of zero bytes is decoded (every byte read as 0xFF,
+// ISO/IEC 15444-1 C.3.4) instead of rejected as decode/t1.rs:109-111 does.
 std::vector<int32_t> decode_block(const uint8_t* data, size_t n, int w, int h,
-                                  Band band, int mb, int zbp, int npasses) {
+                                  Band band, int mb, int zbp, int npasses, bool allow_empty) {
   init_tables();
   std::vector<int32_t> outc((size_t)w * h, 0);
   if (npasses == 0) return outc;
-  if (n == 0) throw Error(kDecodeFailed, "non-empty code-block has no compressed bytes");
+  if (n == 0 && !allow_empty) throw Error(kDecodeFailed, "non-empty code-block has no compressed bytes");
   if (zbp > mb) throw Error(kDecodeFailed, "zero-bitplane count exceeds subband bit-plane count");
   int mbp = mb - zbp;
   if (mbp == 0) throw Error(kDecodeFailed, "non-empty code-block has no magnitude bit-planes");

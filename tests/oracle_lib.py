@@ -161,13 +161,15 @@ class Oracle:
         self._err(rc, "orc_block_summary")
         return rows[:9 * n.value].reshape(-1, 9)
 
-    def decode(self, data, rct_chroma_extra_bitplane=False):
+    def decode(self, data, rct_chroma_extra_bitplane=False, accept_empty_segments=False):
         """The reference's decoder (src/decode/*.rs); with
         rct_chroma_extra_bitplane, RCT chroma code-blocks are read with the
         extra bit-plane their encoder gave them (backend.rs:179-189), which
-        the reference's decoder does not do."""
+        the reference's decoder does not do; with accept_empty_segments, a
+        code-block with passes but no bytes is decoded from an all-0xFF
+        stream instead of rejected (decode/t1.rs:109-111)."""
         w, h, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int()
-        flag = int(bool(rct_chroma_extra_bitplane))
+        flag = int(bool(rct_chroma_extra_bitplane)) | (2 if accept_empty_segments else 0)
         rc = self.lib.orc_decode_ex(data, ctypes.c_size_t(len(data)), flag, ctypes.byref(w), ctypes.byref(h),
                                     ctypes.byref(c), None, ctypes.c_size_t(0))
         self._err(rc, "orc_decode")

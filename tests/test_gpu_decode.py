@@ -8,6 +8,8 @@ operations in its order, without contraction). Corrupted files either fail
 on the host (both decoders) or decode to the same samples. The gray
 lossless 32x32 pattern is the reference's own end-to-end test
 (src/decode/mod.rs:486-508)."""
+import re
+
 import numpy as np
 import pytest
 
@@ -47,12 +49,27 @@ CASES = [
 ]
 
 
+def _same_failure(eng, orc, data, **flags):
+    """Decodes with both decoders; when the oracle rejects the file the
+    device decoder must reject it with the same message. Returns the
+    oracle's samples, or None."""
+    try:
+        return orc.decode(data, **flags)
+    except RuntimeError as e:
+        msg = re.escape(str(e).split(": ", 2)[-1])
+        with pytest.raises((jl.DecodeFailed, jl.UnsupportedFeature), match=msg):
+            eng.decode(data, **flags)
+        return None
+
+
 @pytest.mark.parametrize("w,h,c,q", CASES)
 def test_decode_equals_the_oracle(eng, orc, w, h, c, q):
     px = synth_page(w, h, c, 70 + w + q, photo_w=max(w // 3, 1), photo_h=max(h // 3, 1))
     data = eng.encode(px, w, h, c, q, (w + q) % 2)
-    got, gw, gh, gc = eng.decode(data)
-    ow, oh, oc, want = orc.decode(data)
+    _same_failure(eng, orc, data)
+    flags = dict(accept_empty_segments=True)
+    got, gw, gh, gc = eng.decode(data, **flags)
+    ow, oh, oc, want = orc.decode(data, **flags)
     assert (gw, gh, gc) == (ow, oh, oc) == (w, h, c)
     got = np.frombuffer(got, np.uint8)
     if not np.array_equal(got, want):
@@ -118,3 +135,58 @@ def test_corrupted_payload_decodes_like_the_oracle(eng, orc, seed):
     else:
         got, _, _, _ = eng.decode(data)
         assert np.array_equal(np.frombuffer(got, np.uint8), want)
+
+
+def test_decode_batch_equals_the_oracle_per_file(eng, orc):
+    # mixed sizes, gray/sRGB, lossless/lossy, J2K/JP2 in one call; a broken
+    # file fails alone
+    shapes = [(64, 64, 1, 100), (333, 211, 3, 75), (1275, 1650, 1, 85), (7, 3, 3, 40), (640, 480, 3, 100),
+              (2550, 3300, 3, 62), (100, 70, 1, 50), (257, 129, 1, 95)]
+    files, pxs = [], []
+    for i, (w, h, c, q) in enumerate(shapes):
+        px = synth_page(w, h, c, 300 + i, photo_w=max(w // 3, 1), photo_h=max(h // 3, 1))
+        pxs.append(px)
+        files.append(eng.encode(px, w, h, c, q, i % 2))
+    files.insert(3, files[2][:len(files[2]) // 3])
+    flags = dict(rct_chroma_extra_bitplane=True, accept_empty_segments=True)
+    got = eng.decode_batch(files, **flags)
+    assert isinstance(got[3], (jl.DecodeFailed, jl.UnsupportedFeature))
+    del got[3], files[3]
+    for (w, h, c, q), px, f, g in zip(shapes, pxs, files, got):
+        assert not isinstance(g, Exception), g
+        data, gw, gh, gc = g
+        assert (gw, gh, gc) == (w, h, c)
+        want = orc.decode(f, **flags)[3]
+        assert np.array_equal(np.frombuffer(data, np.uint8), want)
+        if q >= 100:
+            assert np.array_equal(want, px)
+    imgs = jl.decode_batch(files[:2], engine=eng, **flags)
+    assert [im.width for im in imgs] == [64, 333]
+
+
+@pytest.mark.parametrize("w,h,c,q,seed", [(7, 3, 3, 40, 303), (257, 129, 1, 95, 307)])
+def test_empty_segments_fail_like_the_reference_unless_accepted(eng, orc, w, h, c, q, seed):
+    # the encoder keeps a single cleanup pass whose MQ byte count is 0 for
+    # some blocks; the reference's decoder rejects such a block
+    # (decode/t1.rs:109-111), and so does this one unless asked to accept it
+    px = synth_page(w, h, c, seed, photo_w=max(w // 3, 1), photo_h=max(h // 3, 1))
+    data = eng.encode(px, w, h, c, q, 0)
+    assert data == orc.encode(px, w, h, c, q, fmt=0)
+    assert _same_failure(eng, orc, data) is None
+    got = eng.decode(data, accept_empty_segments=True)[0]
+    assert np.array_equal(np.frombuffer(got, np.uint8), orc.decode(data, accept_empty_segments=True)[3])
+
+
+def test_decode_batch_splits_rounds_under_a_small_budget(eng, orc):
+    # 6 files of about 8.3 MB of device state each under a 24 MiB budget:
+    # rounds of two, retried smaller when a pool cannot grow
+    pages = [synth_page(640, 480, 3, 900 + i, photo_w=200, photo_h=150) for i in range(6)]
+    files = [eng.encode(p, 640, 480, 3, 70, 0) for p in pages]
+    small = jl.Engine(0, hbm_budget_bytes=24 << 20)
+    try:
+        got = small.decode_batch(files)
+        for f, g in zip(files, got):
+            assert not isinstance(g, Exception), g
+            assert np.array_equal(np.frombuffer(g[0], np.uint8), orc.decode(f)[3])
+    finally:
+        small.close()

@@ -546,3 +546,23 @@ def test_rgb_lossless_chroma_needs_the_extra_bitplane_to_decode(orc):
         assert np.array_equal(dec, px)
     gray = np.arange(64 * 64, dtype=np.uint32).astype(np.uint8)
     assert np.array_equal(orc.decode(orc.encode(gray, 64, 64, 1, 100, fmt=1))[3], gray)
+
+
+def test_empty_segment_blocks_are_rejected_by_the_reference_decoder(orc):
+    """Some lossy outputs keep a single cleanup pass whose MQ byte count is 0
+    (the pass's rate in the R-D curve), so the packet carries a code-block
+    with one pass and no bytes. The reference's decoder rejects it
+    (decode/t1.rs:109-111); decoded from an all-0xFF stream (C.3.4) it reads
+    back like its neighbours."""
+    from jp2lam_gb300._native import synth_page
+    for w, h, c, q, seed in ((7, 3, 3, 40, 303), (257, 129, 1, 95, 307)):
+        px = synth_page(w, h, c, seed, photo_w=max(w // 3, 1), photo_h=max(h // 3, 1))
+        rows = orc.block_summary(px, w, h, c, q)
+        assert ((rows[:, 7] == 1) & (rows[:, 8] == 0)).any()
+        data = orc.encode(px, w, h, c, q, fmt=0)
+        with pytest.raises(RuntimeError, match="no compressed bytes"):
+            orc.decode(data)
+        dw, dh, dc, dec = orc.decode(data, accept_empty_segments=True)
+        assert (dw, dh, dc) == (w, h, c)
+        err = np.abs(dec.astype(int) - px.astype(int))
+        assert err.mean() < 16
