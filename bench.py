@@ -25,7 +25,9 @@ Beside the headline, the same run measures the batched and served paths
             one jp2g_encode_device per page (--uneven-pages);
   decode  : jp2g_decode of 2550x3300 gray q85, sRGB q75 and gray lossless
             codestreams (host bytes in, samples out), beside the oracle's
-            single-threaded decoder on the same bytes (--no-decode);
+            single-threaded decoder on the same bytes, and one
+            jp2g_decode_batch call over a 64-page sRGB q75 batch's outputs
+            (--no-decode, --decode-batch-pages);
   served  : Poisson arrivals of a 70% uneven-page / 30% 256x256 gray q60
             thumbnail mix through jp2g_submit/jp2g_poll under a 40 GB device
             budget: an offered-rate sweep (4 s per rate, extended upward while
@@ -476,6 +478,26 @@ def bench_decode(eng, args):
                       "ms_min": float(np.min(times)) * 1e3, "bytes": len(data),
                       "cpu_oracle_mpix_per_s": W * H / 1e6 / cpu_s, "cpu_cores": 1,
                       "equal_to_oracle": bool(np.array_equal(np.frombuffer(got, np.uint8), want))}
+    if args.decode_batch_pages > 0:
+        # the batched parity loop: every output of a 64-page sRGB q75 batch
+        # decoded in one jp2g_decode_batch call (files in host memory,
+        # samples back in host memory); two of them checked against the oracle
+        pages = _rgb_pages(args.decode_batch_pages, 7000)
+        files = eng.encode_batch(pages)
+        flags = dict(accept_empty_segments=True)
+        got = eng.decode_batch(files, **flags)
+        times = []
+        for _ in range(max(args.decode_steps // 3, 2)):
+            t0 = time.perf_counter()
+            got = eng.decode_batch(files, **flags)
+            times.append(time.perf_counter() - t0)
+        mpix = sum(p["w"] * p["h"] for p in pages) / 1e6
+        sec = float(np.median(times))
+        checked = [bool(np.array_equal(np.frombuffer(got[i][0], np.uint8), orc.decode(files[i], **flags)[3]))
+                   for i in (0, len(files) - 1)]
+        legs["batch_srgb_q75"] = {"pages": len(pages), "e2e_mpix_per_s": mpix / sec, "ms_median": sec * 1e3,
+                                  "pages_per_s": len(pages) / sec, "failed": sum(isinstance(g, Exception) for g in got),
+                                  "checked_against_oracle": checked}
     return legs
 
 
@@ -504,7 +526,11 @@ def _compact_legs(detail):
     d = detail.get("decode")
     if d:
         out["decode"] = {k: {"e2e": _r(v["e2e_mpix_per_s"]), "cpu_oracle": _r(v["cpu_oracle_mpix_per_s"]),
-                             "equal": v["equal_to_oracle"]} for k, v in d.items()}
+                             "equal": v["equal_to_oracle"]} for k, v in d.items() if "cpu_oracle_mpix_per_s" in v}
+        if "batch_srgb_q75" in d:
+            b = d["batch_srgb_q75"]
+            out["decode"]["batch_srgb_q75"] = {"e2e": _r(b["e2e_mpix_per_s"]), "pages": b["pages"],
+                                               "equal": all(b["checked_against_oracle"]) and b["failed"] == 0}
         out["decode"]["unit"] = "MPix/s"
     v = detail.get("served")
     if v:
@@ -533,6 +559,7 @@ def main():
     ap.add_argument("--no-decode", action="store_true")
     ap.add_argument("--only-decode", action="store_true", help="run only the decode leg; prints its object")
     ap.add_argument("--decode-steps", type=int, default=10)
+    ap.add_argument("--decode-batch-pages", type=int, default=64)
     ap.add_argument("--no-autotune", action="store_true",
                     help="time the batched and uneven workloads under the default options")
     ap.add_argument("--batch-pages", type=int, default=64)

@@ -1326,7 +1326,7 @@ int jp2g_encode_with_psnr(jp2g_ctx* c, const uint8_t* px, uint32_t w, uint32_t h
 // decoding launch over all their code-blocks, one inverse-DWT launch pair
 // per level over all their components, and one launch for the samples
 // (t1dec.cu, recon.cu). Rounds are sized by device memory (the context's
-// budget, else 8 GiB of planes); a round that does not fit is split.
+// budget, else 24 GiB); a round whose pools cannot grow is split.
 namespace {
 
 struct DecodePage {
@@ -1464,7 +1464,7 @@ int decode_round(jp2g_ctx* c, std::vector<DecodePage>& pg, const std::vector<siz
 // grow within the budget.
 int decode_rounds(jp2g_ctx* c, std::vector<DecodePage>& pg, std::vector<size_t> ids, const uint8_t* const* bytes,
                   const size_t* lens, uint8_t** outs, size_t* out_lens) {
-  const uint64_t cap = c->budget ? c->budget : (uint64_t)9 << 30;
+  const uint64_t cap = c->budget ? c->budget : (uint64_t)24 << 30;
   size_t k = 0;
   while (k < ids.size()) {
     std::vector<size_t> round;
