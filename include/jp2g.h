@@ -190,10 +190,11 @@ int jp2g_cancel(jp2g_ctx* ctx, uint64_t ticket);
  *                             they take, the rest being coded 32 to a warp
  *                             (0 = all blocks);
  * JP2G_OPT_MQ_CHAINS_PER_PAIR with pipelines: code-blocks each pair codes at
- *                             once, 1 (all lanes of a warp on one chain) or 2
+ *                             once, 1 (all lanes of a warp on one chain), 2
  *                             (one per half-warp: about half the issue slots
- *                             per symbol); 0 = automatic (1 up to 8 blocks
- *                             per SM, else 2). */
+ *                             per symbol) or 4 (one per quarter-warp); 0 =
+ *                             automatic (1 up to 8 blocks per SM, 2 up to 24,
+ *                             else 4 on 4 pairs per SM). */
 enum {
   JP2G_OPT_WAVE_BLOCKS = 0,
   JP2G_OPT_MQ_BLOCKS_PER_WARP = 1,

@@ -418,13 +418,14 @@ int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live, bool raw) {
 
 // Code-blocks each MQ producer/consumer pair codes at once. Automatic: one
 // (all lanes on the chain) up to 8 blocks per SM, where the heaviest
-// block's chain sets the time; two (one per half-warp) above, where
-// instruction issue does (measured on gray pages of 1275x1650 to 3400x4400
-// and a 2550x3300 sRGB page).
+// block's chain sets the time; two (one per half-warp) up to 24, where
+// instruction issue does; four (one per quarter-warp, on 4 pairs per SM)
+// above (measured on gray pages of 1275x1650 to 3400x4400 and 2550x3300
+// sRGB pages: 4.5 against 5.6 ms of MQ for the sRGB page).
 int mq_chains_per_pair(const jp2g_ctx* c, uint32_t nb) {
   const int64_t v = c->opt[JP2G_OPT_MQ_CHAINS_PER_PAIR];
-  if (v == 1 || v == 2) return (int)v;
-  return nb <= (uint32_t)c->num_sms * 8u ? 1 : 2;
+  if (v == 1 || v == 2 || v == 4) return (int)v;
+  return nb <= (uint32_t)c->num_sms * 8u ? 1 : (nb <= (uint32_t)c->num_sms * 24u ? 2 : 4);
 }
 
 // Runs f(0..n-1) on up to `threads` host threads.
@@ -881,9 +882,13 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
   // pulling and packed warps.
   const int64_t pipes_opt = c->opt[JP2G_OPT_MQ_PIPES_PER_SM];
   const bool use_pipe = use_pull && (pipes_opt > 0 || (pipes_opt == 0 && nb <= sms * 48u));
-  if (use_pipe)
-    launch_t1_mq_pipe(ta, c->num_sms, pipes_opt > 0 ? (int)pipes_opt : 8, mq_chains_per_pair(c, nb),
+  if (use_pipe) {
+    // four chains per pair run on 4 pairs per SM (16 chains per SM, as 8
+    // pairs of two): measured best for an sRGB 2550x3300 page
+    const int chains = mq_chains_per_pair(c, nb);
+    launch_t1_mq_pipe(ta, c->num_sms, pipes_opt > 0 ? (int)pipes_opt : (chains == 4 ? 4 : 8), chains,
                       (uint32_t)c->opt[JP2G_OPT_MQ_HEAVY], dptr<uint32_t>(c->stats) + 2, c->stream);
+  }
   else if (use_pull)
     launch_t1_mq_pull(ta, c->num_sms, pull, dptr<uint32_t>(c->stats) + 2, c->stream);
   else
@@ -1816,7 +1821,8 @@ int jp2g_set_option(jp2g_ctx* c, int option, int64_t value) {
       if (value < 0 || value > 0xffffffffll) return set_err(c, JP2G_INVALID_INPUT, "mq_heavy must be >= 0");
       break;
     case JP2G_OPT_MQ_CHAINS_PER_PAIR:
-      if (value < 0 || value > 2) return set_err(c, JP2G_INVALID_INPUT, "mq_chains_per_pair must be 0..2");
+      if (value < 0 || value > 4 || value == 3)
+        return set_err(c, JP2G_INVALID_INPUT, "mq_chains_per_pair must be 0, 1, 2 or 4");
       break;
     default:
       return set_err(c, JP2G_INVALID_INPUT, "unknown option " + std::to_string(option));
@@ -1902,8 +1908,9 @@ int jp2g_autotune(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, int repeats
   // pulling; blocks packed per warp)
   struct Mq { int64_t bpw, wps, pipes, chains; };
   const Mq mq[] = {{0, 0, 0, 0},   {1, 0, 4, 1},   {1, 0, 8, 1},   {1, 0, 16, 1}, {1, 0, 4, 2},
-                   {1, 0, 8, 2},   {1, 0, 16, 2},  {1, 8, -1, 0},  {1, 12, -1, 0}, {1, 16, -1, 0},
-                   {2, 0, 0, 0},   {4, 0, 0, 0},   {8, 0, 0, 0},   {16, 0, 0, 0}, {32, 0, 0, 0}};
+                   {1, 0, 8, 2},   {1, 0, 16, 2},  {1, 0, 4, 4},   {1, 0, 8, 4},  {1, 8, -1, 0},
+                   {1, 12, -1, 0}, {1, 16, -1, 0}, {2, 0, 0, 0},   {4, 0, 0, 0},  {8, 0, 0, 0},
+                   {16, 0, 0, 0},  {32, 0, 0, 0}};
   int64_t cur[JP2G_NUM_OPTS], win[JP2G_NUM_OPTS];
   std::memcpy(cur, saved, sizeof cur);
   cur[JP2G_OPT_MQ_HEAVY] = 0;

@@ -1169,14 +1169,16 @@ void launch_t1_mq_pipe(const T1Args& a, int num_sms, int pipes_per_sm, int chain
   if (a.nblocks == 0) return;
   cudaMemsetAsync(next, 0, sizeof(uint32_t), st);
   heavy = heavy == 0 ? a.nblocks : std::min(heavy, a.nblocks);
-  chains = chains == 2 ? 2 : 1;
+  chains = chains == 2 || chains == 4 ? chains : 1;
   const uint32_t per_pipe_cta = (uint32_t)kPipes * (uint32_t)chains;  // blocks a CTA codes at once
   const uint32_t pipe_ctas = std::max<uint32_t>(
       1u, std::min<uint32_t>((uint32_t)num_sms * (uint32_t)pipes_per_sm / kPipes,
                              (heavy + per_pipe_cta - 1) / per_pipe_cta));
   const uint32_t per_cta = kPipes * 2 * 32;
   const uint32_t packed_ctas = (a.nblocks - heavy + per_cta - 1) / per_cta;
-  if (chains == 2)
+  if (chains == 4)
+    t1_mq_pipe_kernel<4><<<pipe_ctas + packed_ctas, kPipes * 64, 0, st>>>(a, next, pipe_ctas, heavy);
+  else if (chains == 2)
     t1_mq_pipe_kernel<2><<<pipe_ctas + packed_ctas, kPipes * 64, 0, st>>>(a, next, pipe_ctas, heavy);
   else
     t1_mq_pipe_kernel<1><<<pipe_ctas + packed_ctas, kPipes * 64, 0, st>>>(a, next, pipe_ctas, heavy);
