@@ -20,8 +20,11 @@ from jp2lam_gb300._native import synth_page
 
 pytestmark = pytest.mark.gpu
 
+# the last two: a reversible quality above 100 (every quality >= 100 takes
+# the 5/3 path), and an image exactly at the scratch limit
+# (ceil(w/2) * ceil(h/2) * ncomp = 1,048,576)
 CASES = [(700, 500, 3, 85), (640, 480, 1, 100), (257, 129, 1, 20), (96, 64, 3, 100), (7, 5, 1, 50),
-         (1, 9, 3, 85)]
+         (1, 9, 3, 85), (200, 150, 3, 180), (2048, 2048, 1, 85)]
 
 
 def _noalloc(lib, d_px, w, h, c, q, d_out, stream):
@@ -55,7 +58,8 @@ def test_noalloc_rejects_images_beyond_its_scratch():
     import torch
     lib = _native.load_library()
     d = torch.empty(16, dtype=torch.int32, device="cuda")
-    rc = lib.jp2g_dwt_noalloc(ctypes.c_void_p(d.data_ptr()), 4096, 4096, 1, 85,
-                              ctypes.c_void_p(d.data_ptr()), None)
-    assert rc == jl.InvalidInput.code
-    assert b"allocation-free" in lib.jp2g_last_error(None)
+    for w, h, c in ((4096, 4096, 1), (2050, 2048, 1), (1184, 1184, 3)):  # and just past the limit
+        rc = lib.jp2g_dwt_noalloc(ctypes.c_void_p(d.data_ptr()), w, h, c, 85,
+                                  ctypes.c_void_p(d.data_ptr()), None)
+        assert rc == jl.InvalidInput.code
+        assert b"allocation-free" in lib.jp2g_last_error(None)
