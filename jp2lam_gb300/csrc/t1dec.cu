@@ -136,26 +136,33 @@ struct BlockDecoder {
   const uint8_t* zc;
   uint64_t wmask;
 
+  // A pass loads (and writes back) only the masks it uses: significance
+  // and visited always, signs for the passes that decode signs, refined for
+  // the refinement pass (fewer live registers, more decoders per SM).
+  template <bool kSigns, bool kRefined>
   __device__ void load(int k, Stripe& t) const {
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
       t.S[i] = s.sig[k + i];
-      t.G[i] = s.sgn[k + i];
+      if (kSigns) t.G[i] = s.sgn[k + i];
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       t.V[i] = s.vis[k + 1 + i];
-      t.R[i] = s.ref[k + 1 + i];
+      if (kRefined) t.R[i] = s.ref[k + 1 + i];
       t.B[i] = 0;
     }
   }
+  template <bool kSigns, bool kRefined>
   __device__ void store(int k, const Stripe& t) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      s.sig[k + 1 + i] = t.S[i + 1];
-      s.sgn[k + 1 + i] = t.G[i + 1];
-      s.vis[k + 1 + i] = t.V[i];
-      s.ref[k + 1 + i] = t.R[i];
+      if (kSigns) {  // the passes that can make samples significant
+        s.sig[k + 1 + i] = t.S[i + 1];
+        s.sgn[k + 1 + i] = t.G[i + 1];
+        s.vis[k + 1 + i] = t.V[i];
+      }
+      if (kRefined) s.ref[k + 1 + i] = t.R[i];
       s.bits[k + i] |= t.B[i];
     }
   }
@@ -210,7 +217,7 @@ struct BlockDecoder {
 
   __device__ void sigpass(int k, int lim) {
     Stripe t;
-    load(k, t);
+    load<true, false>(k, t);
     uint64_t cols = sig_candidates(t, lim);
     while (cols) {
       const int x = __ffsll((long long)cols) - 1;
@@ -222,7 +229,7 @@ struct BlockDecoder {
       cols &= above(x);
       if (grew) cols = sig_candidates(t, lim) & above(x);
     }
-    store(k, t);
+    store<true, false>(k, t);
   }
 
   template <int r>
@@ -235,7 +242,7 @@ struct BlockDecoder {
 
   __device__ void refpass(int k, int lim) {
     Stripe t;
-    load(k, t);
+    load<false, true>(k, t);
     uint64_t cols = 0;
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -250,7 +257,7 @@ struct BlockDecoder {
       if (lim > 3) ref_one<3>(t, x, bx);
       cols &= above(x);
     }
-    store(k, t);
+    store<false, true>(k, t);
   }
 
   template <int r>
@@ -265,7 +272,7 @@ struct BlockDecoder {
 
   __device__ void cleanup(int k, int lim) {
     Stripe t;
-    load(k, t);
+    load<true, false>(k, t);
     uint64_t busy = 0;
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -313,7 +320,7 @@ struct BlockDecoder {
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) t.V[r] = 0;
-    store(k, t);
+    store<true, false>(k, t);
   }
 };
 
