@@ -6,6 +6,7 @@ back to anything else: a missing library or a missing GPU raises.
 from __future__ import annotations
 
 import ctypes
+import weakref
 import os
 import threading
 
@@ -224,8 +225,9 @@ class Engine:
 
     def decode(self, data: bytes, rct_chroma_extra_bitplane: bool = False, accept_empty_segments: bool = False):
         """(pixels, w, h, ncomp): a J2K/JP2 file decoded on the device
-        (decode_jp2, src/decode/mod.rs:56-61); pixels interleaved. The two
-        options relax the reference decoder's checks (include/jp2g.h)."""
+        (decode_jp2, src/decode/mod.rs:56-61); pixels interleaved, as a uint8
+        array over the library's buffer. The two options relax the reference
+        decoder's checks (include/jp2g.h)."""
         buf = np.frombuffer(bytes(data), dtype=np.uint8)
         out = _u8p()
         n = ctypes.c_size_t()
@@ -236,13 +238,11 @@ class Engine:
                                       ctypes.byref(out), ctypes.byref(n),
                                       ctypes.byref(w), ctypes.byref(h), ctypes.byref(c))
             self._check(rc)
-        px = ctypes.string_at(out, n.value)
-        self.lib.jp2g_free(out)
-        return px, w.value, h.value, c.value
+        return self._owned(out, n.value), w.value, h.value, c.value
 
     def decode_batch(self, files, rct_chroma_extra_bitplane: bool = False, accept_empty_segments: bool = False):
         """jp2g_decode_batch: a list with, per file, (pixels, w, h, ncomp) or
-        the Jp2LamError it failed with."""
+        the Jp2LamError it failed with; pixels as in decode."""
         n = len(files)
         if n == 0:
             return []
@@ -262,11 +262,20 @@ class Engine:
         res = []
         for i in range(n):
             if status[i] == 0:
-                res.append((ctypes.string_at(outs[i], out_lens[i]), ws[i], hs[i], cs[i]))
-                self.lib.jp2g_free(ctypes.cast(outs[i], _u8p))
+                res.append((self._owned(ctypes.cast(outs[i], _u8p), out_lens[i]), ws[i], hs[i], cs[i]))
             else:
                 res.append(_BY_CODE.get(status[i], EncodeFailed)(msg))
         return res
+
+    def _owned(self, ptr, n: int) -> np.ndarray:
+        """A uint8 array over a buffer the library returned, without a copy;
+        the buffer goes back to jp2g_free when the array is collected."""
+        if n == 0:
+            self.lib.jp2g_free(ptr)
+            return np.zeros(0, np.uint8)
+        arr = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_uint8)), shape=(n,))
+        weakref.finalize(arr, self.lib.jp2g_free, ptr)
+        return arr
 
     def encode_device(self, dev_ptr: int, w: int, h: int, ncomp: int, quality: int, fmt: int) -> bytes:
         out = _u8p()
