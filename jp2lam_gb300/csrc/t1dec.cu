@@ -107,12 +107,19 @@ struct MqDecoder {
         return mps;
       }
     }
-    do {
-      if (ct == 0) bytein();
-      a <<= 1;
-      c <<= 1;
-      --ct;
-    } while (a < 0x8000u);
+    // renormalise: shift until a >= 0x8000, reading a byte whenever the bit
+    // count runs out first (the one-bit-at-a-time loop of C.3.3, in runs)
+    uint32_t n = (uint32_t)__clz(a) - 16u;  // 0 < a < 0x8000 here
+    while (n > ct) {
+      a <<= ct;
+      c <<= ct;
+      n -= ct;
+      ct = 0;
+      bytein();
+    }
+    a <<= n;
+    c <<= n;
+    ct -= n;
     return bit;
   }
 };
@@ -179,10 +186,8 @@ struct BlockDecoder {
   template <int r>
   __device__ __forceinline__ void sign(Stripe& t, int x) {
     const uint64_t bx = 1ull << x;
-    const uint32_t ws = x > 0 ? (uint32_t)(t.S[r + 1] >> (x - 1)) & 1u : 0u;
-    const uint32_t wg = x > 0 ? (uint32_t)(t.G[r + 1] >> (x - 1)) & 1u : 0u;
-    const uint32_t es = x < 63 ? (uint32_t)(t.S[r + 1] >> (x + 1)) & 1u : 0u;
-    const uint32_t eg = x < 63 ? (uint32_t)(t.G[r + 1] >> (x + 1)) & 1u : 0u;
+    const uint32_t sw = win3(t.S[r + 1], x), gw = win3(t.G[r + 1], x);  // bit 0 west, bit 2 east
+    const uint32_t ws = sw & 1u, wg = gw & 1u, es = sw >> 2, eg = gw >> 2;
     const uint32_t ns = (uint32_t)(t.S[r] >> x) & 1u, ng = (uint32_t)(t.G[r] >> x) & 1u;
     const uint32_t ss = (uint32_t)(t.S[r + 2] >> x) & 1u, sg = (uint32_t)(t.G[r + 2] >> x) & 1u;
     const uint32_t lu = (ws << 3) | (ws & wg) | (ns << 1) | ((ns & ng) << 4) | (es << 5) | ((es & eg) << 2) |
