@@ -1441,7 +1441,12 @@ int decode_round(jp2g_ctx* c, std::vector<DecodePage>& pg, const std::vector<siz
                "H2D pages") ||
       !cuda_ok(c, cudaMemsetAsync(planes, 0, planes_bytes, c->stream), "memset planes"))
     return JP2G_DECODE_FAILED;
-  launch_t1_decode(dblk, (uint32_t)blk.size(), dptr<uint8_t>(c->t2out), planes, c->stream);
+  // two decoders per warp once the blocks fill the warps the SMs hold at
+  // once (16 per SM) four times over: more chains in flight for batches
+  // (64 sRGB 2550x3300 files: 290 -> 251 ms end to end); one otherwise, so
+  // a file's heaviest chains run alone (one sRGB file: 10.0 against 13.4 ms)
+  const int per_warp = blk.size() > (size_t)c->num_sms * 64u ? 2 : 1;
+  launch_t1_decode(dblk, (uint32_t)blk.size(), dptr<uint8_t>(c->t2out), planes, per_warp, c->stream);
   for (int l = 1; l <= maxl; ++l) launch_idwt_level(djobs + first[l], first[l + 1] - first[l], rows[l], tiles[l], c->stream);
   launch_dec_pixels(dpix, (uint32_t)pix.size(), total_px, c->stream);
   if (!cuda_ok(c, cudaGetLastError(), "decode kernels") ||

@@ -212,8 +212,9 @@ struct PixJob {
   uint64_t npx, pix_base;  // pix_base: the page's first global sample index
   uint32_t ncomp, mct, reversible, pad;
 };
-// Tier-1 decoding of every code-block (t1dec.cu) into zeroed planes.
-void launch_t1_decode(const DecBlock* blocks, uint32_t nblocks, const uint8_t* data, int32_t* planes,
+// Tier-1 decoding of every code-block (t1dec.cu) into zeroed planes, one
+// or two (per_warp) decoders per warp.
+void launch_t1_decode(const DecBlock* blocks, uint32_t nblocks, const uint8_t* data, int32_t* planes, int per_warp,
                       cudaStream_t st);
 // One inverse-DWT level for njobs jobs (recon.cu).
 void launch_idwt_level(const IdwtJob* jobs, uint32_t njobs, uint32_t total_rows, uint32_t total_tiles,

@@ -329,30 +329,38 @@ struct BlockDecoder {
   }
 };
 
+// H decoders per warp: with H = 2 each half-warp decodes its own block
+// (its lane 0 running the chain, its 16 lanes merging), so two chains share
+// a warp's instruction stream: more decoders per SM for batches, at some
+// cost to each chain where the two diverge.
+template <int H>
 __global__ void __launch_bounds__(kDecWarps * 32) t1_decode_kernel(const DecBlock* blocks, uint32_t nblocks,
                                                                      const uint8_t* data, int32_t* planes) {
-  __shared__ WarpState st_all[kDecWarps];
+  constexpr int HL = 32 / H;  // lanes per decoder
+  constexpr int NX = 64 / HL;  // columns each lane merges
+  __shared__ WarpState st_all[kDecWarps * H];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const uint32_t blk = blockIdx.x * kDecWarps + wid;
+  const int half = lane / HL, hl = lane % HL;
+  const uint32_t hmask = H == 1 ? 0xffffffffu : (0xffffu << (16 * half));
+  const uint32_t blk = (blockIdx.x * kDecWarps + wid) * H + half;
   if (blk >= nblocks) return;
-  WarpState& s = st_all[wid];
+  WarpState& s = st_all[wid * H + half];
   const DecBlock d = blocks[blk];
-  for (int i = lane; i < 66; i += 32) s.sig[i] = s.sgn[i] = s.vis[i] = s.ref[i] = 0;
-  for (int i = lane; i < 64; i += 32) s.bits[i] = 0;
+  for (int i = hl; i < 66; i += HL) s.sig[i] = s.sgn[i] = s.vis[i] = s.ref[i] = 0;
+  for (int i = hl; i < 64; i += HL) s.bits[i] = 0;
   // initial context states (src/mq/mod.rs:195-200)
-  if (lane < 20) s.ctx[lane] = lane == kCtxUNI ? 92 : lane == kCtxAGG ? 6 : lane == kCtxZC0 ? 8 : 0;
+  for (int i = hl; i < 20; i += HL) s.ctx[i] = i == kCtxUNI ? 92 : i == kCtxAGG ? 6 : i == kCtxZC0 ? 8 : 0;
   int32_t* plane = planes + d.plane_off;
   const int w = d.w, h = d.h;
-  const int x0 = lane, x1 = lane + 32;
-  __syncwarp();
+  __syncwarp(hmask);
   BlockDecoder dec{s, {}, c_dec.zc + (d.orient & 3) * 512, w == 64 ? ~0ull : (1ull << w) - 1};
-  if (lane == 0 && d.npasses > 0) dec.mq.init(data + d.data_off, d.data_len, s.ctx);
+  if (hl == 0 && d.npasses > 0) dec.mq.init(data + d.data_off, d.data_len, s.ctx);
   // pass sequence: cleanup of the top bit-plane, then significance,
   // refinement and cleanup per bit-plane until the block's passes end
   const int top = (int)d.mb - (int)d.zbp - 1;  // checked on the host: 0..30
   int remaining = d.npasses;
   for (int bp = top; bp >= 0 && remaining > 0; --bp) {
-    if (lane == 0) {
+    if (hl == 0) {
       if (bp < top) {
         for (int k = 0; k < h; k += 4) dec.sigpass(k, min(4, h - k));
         if (--remaining > 0) {
@@ -369,34 +377,37 @@ __global__ void __launch_bounds__(kDecWarps * 32) t1_decode_kernel(const DecBloc
     } else {
       remaining -= bp < top ? min(3, remaining) : 1;
     }
-    __syncwarp();
+    __syncwarp(hmask);
     const int32_t one = (int32_t)(1u << bp);
     for (int y = 0; y < h; ++y) {
-      const uint64_t b = s.bits[y];
-      if (!b) continue;
+      const uint64_t bits = s.bits[y];
+      if (!bits) continue;
       int32_t* row = plane + (size_t)y * d.stride;
-      if (x0 < w && ((b >> x0) & 1u)) row[x0] |= one;
-      if (x1 < w && ((b >> x1) & 1u)) row[x1] |= one;
+#pragma unroll
+      for (int m = 0; m < NX; ++m) {
+        const int x = hl + HL * m;
+        if (x < w && ((bits >> x) & 1u)) row[x] |= one;
+      }
     }
-    __syncwarp();
-    for (int i = lane; i < 64; i += 32) s.bits[i] = 0;
-    __syncwarp();
+    __syncwarp(hmask);
+    for (int i = hl; i < 64; i += HL) s.bits[i] = 0;
+    __syncwarp(hmask);
   }
   // signed coefficients, or their midpoint dequantised values
   for (int y = 0; y < h; ++y) {
     const uint64_t neg = s.sgn[y + 1];
     int32_t* row = plane + (size_t)y * d.stride;
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const int x = j ? x1 : x0;
+    for (int m = 0; m < NX; ++m) {
+      const int x = hl + HL * m;
       if (x >= w) continue;
-      const int32_t m = row[x];
+      const int32_t mag = row[x];
       const bool n = (neg >> x) & 1u;
       if (d.reversible) {
-        row[x] = n ? -m : m;
+        row[x] = n ? -mag : mag;
       } else {
         float v = 0.0f;
-        if (m != 0) v = __fmul_rn(__fmul_rn(n ? -1.0f : 1.0f, __fadd_rn((float)(uint32_t)m, 0.5f)), d.step);
+        if (mag != 0) v = __fmul_rn(__fmul_rn(n ? -1.0f : 1.0f, __fadd_rn((float)(uint32_t)mag, 0.5f)), d.step);
         row[x] = __float_as_int(v);
       }
     }
@@ -414,10 +425,16 @@ bool upload_decode_tables(const uint8_t* zc, const uint8_t* sc, const uint8_t* s
   return cudaMemcpyToSymbol(c_dec, &t, sizeof t) == cudaSuccess;
 }
 
-void launch_t1_decode(const DecBlock* blocks, uint32_t nblocks, const uint8_t* data, int32_t* planes,
+void launch_t1_decode(const DecBlock* blocks, uint32_t nblocks, const uint8_t* data, int32_t* planes, int per_warp,
                       cudaStream_t st) {
   if (nblocks == 0) return;
-  t1_decode_kernel<<<(nblocks + kDecWarps - 1) / kDecWarps, kDecWarps * 32, 0, st>>>(blocks, nblocks, data, planes);
+  if (per_warp == 2) {
+    const uint32_t per_cta = kDecWarps * 2;
+    t1_decode_kernel<2><<<(nblocks + per_cta - 1) / per_cta, kDecWarps * 32, 0, st>>>(blocks, nblocks, data, planes);
+  } else {
+    t1_decode_kernel<1><<<(nblocks + kDecWarps - 1) / kDecWarps, kDecWarps * 32, 0, st>>>(blocks, nblocks, data,
+                                                                                           planes);
+  }
 }
 
 }  // namespace jp2g
