@@ -190,3 +190,19 @@ def test_decode_batch_splits_rounds_under_a_small_budget(eng, orc):
             assert np.array_equal(np.frombuffer(g[0], np.uint8), orc.decode(f)[3])
     finally:
         small.close()
+
+
+def test_large_decode_batch_two_decoders_per_warp(eng, orc):
+    # over 9,728 code-blocks in one call: the decoders run two per warp;
+    # every file must equal its own single-file decode and the oracle
+    pages = [(2550, 3300, 3, 75), (2550, 3300, 3, 50), (1275, 1650, 1, 85)]
+    files = []
+    for i, (w, h, c, q) in enumerate(pages):
+        px = synth_page(w, h, c, 500 + i, photo_w=w // 3, photo_h=h // 3)
+        files.append(eng.encode(px, w, h, c, q, 1))
+    flags = dict(accept_empty_segments=True)
+    got = eng.decode_batch(files, **flags)
+    for f, g in zip(files, got):
+        assert not isinstance(g, Exception), g
+        assert np.array_equal(np.asarray(g[0]), np.asarray(eng.decode(f, **flags)[0]))
+    assert np.array_equal(np.asarray(got[1][0]), orc.decode(files[1], **flags)[3])
