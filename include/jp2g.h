@@ -168,7 +168,8 @@ int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, in
 int jp2g_cancel(jp2g_ctx* ctx, uint64_t ticket);
 
 /* Tuning knobs (the autotuner sets these):
- * JP2G_OPT_WAVE_BLOCKS        most code-blocks per device wave (default 160000;
+ * JP2G_OPT_WAVE_BLOCKS        most code-blocks per device wave (default 240000,
+ *                             160000 under a memory budget;
  *                             waves never exceed 246,723 64x64 blocks or
  *                             838,860 32x32 blocks, whose payload slots need
  *                             32-bit offsets);

@@ -116,7 +116,9 @@ struct jp2g_ctx {
   cudaEvent_t ev[kNumEvents] = {};
   float stage_ms[kNumStages + 4] = {};
   uint64_t counters[8] = {};
-  int64_t opt[JP2G_NUM_OPTS] = {160000, 0, 0, 0, 0, 0, 0};
+  // default wave: 240,000 code-blocks (the autotuner's choice on sRGB and
+  // uneven batches: fewer waves, fewer MQ tails); 160,000 under a budget
+  int64_t opt[JP2G_NUM_OPTS] = {240000, 0, 0, 0, 0, 0, 0};
   // submit/poll: a worker thread forms waves from the queue and runs them;
   // a finisher thread marks the finished waves' tickets done.
   std::mutex qmu;
@@ -1150,6 +1152,9 @@ int jp2g_create(jp2g_ctx** out, int device, uint64_t hbm_budget_bytes) {
   jp2g_ctx* c = new jp2g_ctx();
   c->device = device;
   c->budget = hbm_budget_bytes;
+  // under a budget, waves start at 160,000 code-blocks (about 24 GB of
+  // pools for 64x64 blocks) so that the first waves need no split
+  if (hbm_budget_bytes) c->opt[JP2G_OPT_WAVE_BLOCKS] = 160000;
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess || !init_t1_tables()) {
