@@ -10,6 +10,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <functional>
+#include <future>
 #include <cmath>
 #include <limits>
 #include <chrono>
@@ -106,7 +108,7 @@ struct jp2g_ctx {
   std::mutex errmu;
   std::mutex mu;    // device pools and stream: one wave (or encode) at a time
   // device pools
-  DevBuf px, ll0, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
+  DevBuf px, px2, ll0, coef, payload, passes, res, keep, blocks, bands, comps, maxslope, hullp,
       hulls, hulln, offsets, scratch, body, nplanes, planebase, items, itemrec, planes, signs, sym, stats,
       dwtargs, dwtbases, mqorder, mqscratch, recon, reconblk, t2pk, t2bd, t2pg, t2tmpl, t2tree, t2raw, t2hdr,
       t2hdrlen, t2pktoff, t2pagelen, t2pageoff, t2nchunks, t2chunkbase, t2out;
@@ -114,6 +116,12 @@ struct jp2g_ctx {
   HostBuf hpx, hpx2, hkeep, hres, hcount, hpageoff, hout;
   bool timing = false;
   cudaEvent_t ev[kNumEvents] = {};
+  // batches: the next wave's pixels go up on copy_stream while the current
+  // wave computes (after its DWT, ev_dwt), into the other pixel buffer
+  // (px / px2); its DWT waits on ev_up
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_dwt[2] = {}, ev_up[2] = {};
+  uint8_t* wave_px = nullptr;  // the current wave's device pixels
   float stage_ms[kNumStages + 4] = {};
   uint64_t counters[8] = {};
   // default wave: 240,000 code-blocks (the autotuner's choice on sRGB and
@@ -331,7 +339,7 @@ int run_dwt_wave(jp2g_ctx* c, const std::vector<PageJob*>& live, bool raw) {
   if (ll_total > 0 && !reserve(c, c->ll0, ll_total * 4)) return kEncodeFailed;
   int32_t* coef = dptr<int32_t>(c->coef);
   auto page_px = [&](size_t i) {
-    return live[i]->dev_px ? live[i]->dev_px : dptr<uint8_t>(c->px) + live[i]->px_off;
+    return live[i]->dev_px ? live[i]->dev_px : c->wave_px + live[i]->px_off;
   };
   int launches = 0;
   // pages with no decomposition level: copy (and quantise) into blocks
@@ -468,6 +476,9 @@ struct WaveDebug {
 struct Prestaged {
   HostBuf* buf;
   size_t total;
+  DevBuf* dev = nullptr;              // the wave's device pixel buffer (default: px)
+  cudaEvent_t uploaded = nullptr;     // set: the pixels are already on their way (wait on it)
+  std::function<void()> after_dwt;    // called once the wave's DWT is launched
 };
 constexpr size_t kStageFailed = ~size_t(0);
 
@@ -792,18 +803,23 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
     if (hpx_total == kStageFailed) return kEncodeFailed;
     staging = reinterpret_cast<const uint8_t*>(c->hpx.p);
   }
-  if (hpx_total > 0) {
-    if (!reserve(c, c->px, hpx_total)) return kEncodeFailed;
+  DevBuf& pxbuf = pre && pre->dev ? *pre->dev : c->px;
+  if (pre && pre->uploaded) {
+    // uploaded on the copy stream while the previous wave computed
+    if (!cuda_ok(c, cudaStreamWaitEvent(c->stream, pre->uploaded, 0), "wait for pixels")) return kEncodeFailed;
+  } else if (hpx_total > 0) {
+    if (!reserve(c, pxbuf, hpx_total)) return kEncodeFailed;
     // one copy per page: from pinned staging, or straight from the caller's
     // memory for small pages in the device layout
     for (PageJob* j : live) {
       if (!j->host_px) continue;
       const uint8_t* from = j->staged ? staging + j->px_off : j->host_px;
-      if (!cuda_ok(c, cudaMemcpyAsync(dptr<uint8_t>(c->px) + j->px_off, from, (size_t)j->w * j->h * j->ncomp,
+      if (!cuda_ok(c, cudaMemcpyAsync(dptr<uint8_t>(pxbuf) + j->px_off, from, (size_t)j->w * j->h * j->ncomp,
                                       cudaMemcpyHostToDevice, c->stream), "H2D"))
         return kEncodeFailed;
     }
   }
+  c->wave_px = dptr<uint8_t>(pxbuf);
   if (!cuda_ok(c, cudaMemcpyAsync(c->blocks.p, blocks.data(), nb * sizeof(BlockDesc),
                                   cudaMemcpyHostToDevice, c->stream), "H2D blocks") ||
       !cuda_ok(c, cudaMemcpyAsync(c->bands.p, bands.data(), bands.size() * sizeof(BandParam),
@@ -814,6 +830,7 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
   record(c, 1);
   // ---- colour + DWT + quantisation, one launch per level for the wave ----
   if (int rc = run_dwt_wave(c, live, dbg && dbg->raw_coefficients)) return rc;
+  if (pre && pre->after_dwt) pre->after_dwt();
   record(c, 2);
   if (dbg && dbg->stop_after_dwt) {
     if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "DWT")) return kEncodeFailed;
@@ -972,7 +989,7 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
 // allocates exactly what it needs under the budget.
 void release_pools(jp2g_ctx* c) {
   cudaStreamSynchronize(c->stream);
-  DevBuf* bufs[] = {&c->px, &c->ll0, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
+  DevBuf* bufs[] = {&c->px, &c->px2, &c->ll0, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
                     &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
@@ -1163,6 +1180,11 @@ int jp2g_create(jp2g_ctx** out, int device, uint64_t hbm_budget_bytes) {
     return JP2G_ENCODE_FAILED;
   }
   for (auto& ev : c->ev) cudaEventCreate(&ev);
+  cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+  for (int k = 0; k < 2; ++k) {
+    cudaEventCreateWithFlags(&c->ev_dwt[k], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_up[k], cudaEventDisableTiming);
+  }
   *out = c;
   return JP2G_OK;
 }
@@ -1179,7 +1201,7 @@ void jp2g_destroy(jp2g_ctx* c) {
   if (c->finisher.joinable()) c->finisher.join();
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
-  DevBuf* bufs[] = {&c->px, &c->ll0, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
+  DevBuf* bufs[] = {&c->px, &c->px2, &c->ll0, &c->coef, &c->payload, &c->passes, &c->res, &c->keep,
                     &c->blocks, &c->bands, &c->comps, &c->maxslope, &c->hullp, &c->hulls, &c->hulln,
                     &c->offsets, &c->scratch, &c->body, &c->nplanes, &c->planebase, &c->items,
                     &c->itemrec, &c->planes, &c->signs, &c->sym, &c->stats, &c->dwtargs, &c->dwtbases,
@@ -1193,6 +1215,14 @@ void jp2g_destroy(jp2g_ctx* c) {
     if (b->p) cudaFreeHost(b->p);
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
+  for (int k = 0; k < 2; ++k) {
+    if (c->ev_dwt[k]) cudaEventDestroy(c->ev_dwt[k]);
+    if (c->ev_up[k]) cudaEventDestroy(c->ev_up[k]);
+  }
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
   cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -1287,7 +1317,7 @@ static int page_metrics(jp2g_ctx* c, const PageJob& j, double* psnr, double* ssi
   r.width = p.width;
   r.height = p.height;
   r.ncomp = p.ncomp;
-  r.px = j.dev_px ? j.dev_px : dptr<uint8_t>(c->px) + j.px_off;
+  r.px = j.dev_px ? j.dev_px : c->wave_px + j.px_off;
   float* f = dptr<float>(c->recon);
   r.stats = reinterpret_cast<double*>(f);  // 16 bytes at the start
   r.plane = f + 4;
@@ -1600,8 +1630,15 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
   // pinned buffer) while wave k is on the device.
   auto waves = form_waves(c, ptrs);
   HostBuf* bufs[2] = {&c->hpx, &c->hpx2};
+  DevBuf* devs[2] = {&c->px, &c->px2};
+  // Without a budget the next wave's pixels also go up to the device while
+  // this wave computes: the helper thread stages them, waits until this
+  // wave's DWT (the last reader of the other pixel buffer two waves back) is
+  // launched, and copies them on the copy stream after it.
+  const bool overlap = c->budget == 0;
   size_t staged = stage_pixels(c, waves.empty() ? nullptr : waves[0].data(),
                                waves.empty() ? 0 : waves[0].size(), *bufs[0]);
+  bool uploaded = false;  // wave w's pixels were sent by the previous wave's helper
   for (size_t w = 0; w < waves.size(); ++w) {
     auto& wave = waves[w];
     if (staged == kStageFailed) {
@@ -1609,17 +1646,56 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
       break;
     }
     size_t next_staged = 0;
+    bool next_uploaded = false;
+    std::promise<bool> dwt_launched;
+    std::future<bool> dwt_future = dwt_launched.get_future();
+    bool signalled = false;
+    DevBuf* next_dev = devs[(w + 1) & 1];
+    bool next_room = false;
+    if (overlap && w + 1 < waves.size()) {
+      // room for the next wave's pixels (an upper bound of what it stages)
+      size_t bound = 0;
+      for (PageJob* j : waves[w + 1])
+        if (j->host_px) bound += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
+      next_room = bound == 0 || reserve(c, *next_dev, bound);
+    }
     std::thread stager;
     if (w + 1 < waves.size()) {
-      stager = std::thread([&, w] {
+      stager = std::thread([&, w, next_dev, next_room] {
         cudaSetDevice(c->device);
-        next_staged = stage_pixels(c, waves[w + 1].data(), waves[w + 1].size(), *bufs[(w + 1) & 1]);
+        auto& nw = waves[w + 1];
+        next_staged = stage_pixels(c, nw.data(), nw.size(), *bufs[(w + 1) & 1]);
+        const bool go = dwt_future.get();
+        if (!go || !next_room || next_staged == kStageFailed || next_staged == 0) return;
+        if (cudaStreamWaitEvent(c->copy_stream, c->ev_dwt[w & 1], 0) != cudaSuccess) return;
+        const uint8_t* pinned = static_cast<const uint8_t*>(bufs[(w + 1) & 1]->p);
+        for (PageJob* j : nw) {
+          if (!j->host_px || j->px_off + (size_t)j->w * j->h * j->ncomp > next_dev->cap) continue;
+          const uint8_t* from = j->staged ? pinned + j->px_off : j->host_px;
+          if (cudaMemcpyAsync(dptr<uint8_t>(*next_dev) + j->px_off, from, (size_t)j->w * j->h * j->ncomp,
+                              cudaMemcpyHostToDevice, c->copy_stream) != cudaSuccess)
+            return;
+        }
+        if (cudaEventRecord(c->ev_up[(w + 1) & 1], c->copy_stream) == cudaSuccess) next_uploaded = true;
       });
     }
-    const Prestaged pre{bufs[w & 1], staged};
+    Prestaged pre{bufs[w & 1], staged};
+    pre.dev = devs[w & 1];
+    pre.uploaded = uploaded ? c->ev_up[w & 1] : nullptr;
+    if (overlap)
+      pre.after_dwt = [&] {
+        if (signalled) return;
+        signalled = true;
+        dwt_launched.set_value(cudaEventRecord(c->ev_dwt[w & 1], c->stream) == cudaSuccess);
+      };
     rc = run_wave_within_budget(c, wave.data(), wave.size(), &pre);
+    if (!signalled) {
+      signalled = true;
+      dwt_launched.set_value(false);  // no DWT was launched: the next wave uploads its own pixels
+    }
     if (stager.joinable()) stager.join();
     staged = next_staged;
+    uploaded = next_uploaded;
     for (int k = 0; k < 8; ++k) counters[k] += c->counters[k];
     if (rc != JP2G_OK) break;
     add_wave_stage_times(c);
