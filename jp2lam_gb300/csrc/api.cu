@@ -1452,7 +1452,7 @@ int decode_round(jp2g_ctx* c, std::vector<DecodePage>& pg, const std::vector<siz
   const size_t blk_bytes = (blk.size() * sizeof(DecBlock) + 255) & ~size_t(255);
   const size_t job_bytes = (jobs.size() * sizeof(IdwtJob) + 255) & ~size_t(255);
   if (!reserve(c, c->reconblk, blk_bytes + job_bytes + pix.size() * sizeof(PixJob) + 256) ||
-      !reserve_host(c, c->hpx, std::max<uint64_t>(nbytes, 16)) || !reserve_host(c, c->hout, std::max<uint64_t>(npxb, 16)))
+      !reserve_host(c, c->hpx, std::max<uint64_t>(nbytes, 16)))
     return JP2G_DECODE_FAILED;
   uint8_t* meta = static_cast<uint8_t*>(c->reconblk.p);
   DecBlock* dblk = reinterpret_cast<DecBlock*>(meta);
@@ -1477,24 +1477,59 @@ int decode_round(jp2g_ctx* c, std::vector<DecodePage>& pg, const std::vector<siz
   launch_t1_decode(dblk, (uint32_t)blk.size(), dptr<uint8_t>(c->t2out), planes, per_warp, c->stream);
   for (int l = 1; l <= maxl; ++l) launch_idwt_level(djobs + first[l], first[l + 1] - first[l], rows[l], tiles[l], c->stream);
   launch_dec_pixels(dpix, (uint32_t)pix.size(), total_px, c->stream);
-  if (!cuda_ok(c, cudaGetLastError(), "decode kernels") ||
-      !cuda_ok(c, cudaMemcpyAsync(c->hout.p, dpx, npxb, cudaMemcpyDeviceToHost, c->stream), "D2H samples") ||
-      !cuda_ok(c, cudaStreamSynchronize(c->stream), "decode"))
+  if (!cuda_ok(c, cudaGetLastError(), "decode kernels")) return JP2G_DECODE_FAILED;
+  if (ids.size() >= 8) {
+    // many files: one read-back into pinned memory, then the host threads
+    // copy each file's samples into its own buffer
+    if (!reserve_host(c, c->hout, std::max<uint64_t>(npxb, 16)) ||
+        !cuda_ok(c, cudaMemcpyAsync(c->hout.p, dpx, npxb, cudaMemcpyDeviceToHost, c->stream), "D2H samples") ||
+        !cuda_ok(c, cudaStreamSynchronize(c->stream), "decode"))
+      return JP2G_DECODE_FAILED;
+    std::atomic<bool> oom{false};
+    parallel_for(ids.size(), host_threads(c), [&](size_t k) {
+      const DecodePage& p = pg[ids[k]];
+      const size_t len = (size_t)p.npx * p.L.ncomp;
+      uint8_t* o = static_cast<uint8_t*>(std::malloc(std::max<size_t>(len, 1)));
+      if (!o) {
+        oom = true;
+        return;
+      }
+      std::memcpy(o, static_cast<const uint8_t*>(c->hout.p) + p.px_base, len);
+      outs[ids[k]] = o;
+      out_lens[ids[k]] = len;
+    });
+    if (!oom) return JP2G_OK;
+    for (size_t i : ids) {
+      std::free(outs[i]);
+      outs[i] = nullptr;
+      out_lens[i] = 0;
+    }
+    return set_err(c, JP2G_DECODE_FAILED, "out of host memory");
+  }
+  // a few files: each file's samples go straight into its own buffer
+  // (pageable copies run near the pinned rate over this GPU's host link)
+  auto drop = [&]() {  // a failed round hands out no buffer
+    for (size_t i : ids) {
+      std::free(outs[i]);
+      outs[i] = nullptr;
+      out_lens[i] = 0;
+    }
     return JP2G_DECODE_FAILED;
-  std::atomic<bool> oom{false};
-  parallel_for(ids.size(), ids.size() >= 8 && npxb >= (8u << 20) ? host_threads(c) : 1, [&](size_t k) {
+  };
+  for (size_t k = 0; k < ids.size(); ++k) {
     const DecodePage& p = pg[ids[k]];
     const size_t len = (size_t)p.npx * p.L.ncomp;
     uint8_t* o = static_cast<uint8_t*>(std::malloc(std::max<size_t>(len, 1)));
     if (!o) {
-      oom = true;
-      return;
+      set_msg(c, "out of host memory");
+      return drop();
     }
-    std::memcpy(o, static_cast<const uint8_t*>(c->hout.p) + p.px_base, len);
     outs[ids[k]] = o;
     out_lens[ids[k]] = len;
-  });
-  if (oom) return set_err(c, JP2G_DECODE_FAILED, "out of host memory");
+    if (!cuda_ok(c, cudaMemcpyAsync(o, dpx + p.px_base, len, cudaMemcpyDeviceToHost, c->stream), "D2H samples"))
+      return drop();
+  }
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "decode")) return drop();
   return JP2G_OK;
 }
 
