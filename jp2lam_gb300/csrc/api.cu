@@ -489,16 +489,22 @@ constexpr size_t kStageFailed = ~size_t(0);
 // others are copied into `buf` (pinned, at the same offsets), planar RGB
 // interleaved on the way (Image::from_rgb_bytes takes RGBRGB), in 2 MiB
 // tasks over the host threads.
-// Host pixels reach the device one copy per page. Pages in the device
-// layout (gray, interleaved RGB) are copied straight from the caller's
-// memory: over this GPU's host link a pageable copy runs at 195 GB/s against
-// 210 GB/s from pinned memory (1 GiB), so gathering into pinned staging
-// first would only add the host copy. Planar RGB is staged: the host
-// threads interleave it into pinned memory on the way.
-bool needs_staging(const PageJob* j) { return j->ncomp == 3 && !j->interleaved; }
+// Host pixels reach the device one copy per page. A wave holding at most
+// kDirectCopyMax bytes of host pixels copies pages in the device layout
+// (gray, interleaved RGB) straight from the caller's memory; a larger wave
+// (a big page, or many pages) is first gathered into pinned staging by the
+// host threads: a pageable copy runs near the pinned rate only for memory
+// the driver has already seen (a first copy of fresh pages is several
+// times slower), and for every wave after a batch's first the gathering
+// overlaps the previous wave's device work. Planar RGB is always staged: it
+// is interleaved on the way.
+constexpr size_t kDirectCopyMax = 32u << 20;
+bool needs_staging(const PageJob* j, size_t wave_host_bytes) {
+  return (j->ncomp == 3 && !j->interleaved) || wave_host_bytes > kDirectCopyMax;
+}
 
 size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
-  size_t total = 0;
+  size_t total = 0, host_bytes = 0;
   std::vector<PageJob*> paged;
   for (size_t i = 0; i < n; ++i) {
     PageJob* j = jobs[i];
@@ -508,11 +514,12 @@ size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
     if (!j->host_px || !build_plan(j->w, j->h, (int)j->ncomp, j->quality, j->format, &p, &f)) continue;
     j->px_off = total;
     total += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
+    host_bytes += (size_t)j->w * j->h * j->ncomp;
     paged.push_back(j);
   }
   std::vector<PageJob*> staged;
   for (PageJob* j : paged)
-    if (needs_staging(j)) {
+    if (needs_staging(j, host_bytes)) {
       j->staged = true;
       staged.push_back(j);
     }
