@@ -317,7 +317,7 @@ __device__ __forceinline__ void emit_column(uint32_t v, uint32_t sm, uint32_t c,
 //    run), so each lane writes its two columns' symbols into the three
 //    streams (SP | MR | cleanup, whose starts are known from the totals) at
 //    offsets from two packed warp scans.
-__global__ void __launch_bounds__(kModelWarps * 32, 6) t1_model_kernel(T1Args a) {
+__global__ void __launch_bounds__(kModelWarps * 32, 5) t1_model_kernel(T1Args a) {
   __shared__ ModelSmem sm_all[kModelWarps];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
