@@ -11,7 +11,6 @@
 #include <algorithm>
 #include <atomic>
 #include <functional>
-#include <future>
 #include <cmath>
 #include <limits>
 #include <chrono>
@@ -73,6 +72,7 @@ struct PageJob {
   uint32_t block_base = 0;  // the page's first code-block in the wave
   size_t px_off = 0;        // the page's pixels in the wave's staging buffer
   bool staged = false;      // copied to the device from pinned staging
+  bool laid_out = false;    // has a place (px_off) in the wave's pixel buffer
   uint8_t* cs = nullptr;  // the finished codestream (J2K or JP2), malloc'd
   size_t cs_len = 0;
   PageJob() = default;
@@ -116,11 +116,11 @@ struct jp2g_ctx {
   HostBuf hpx, hpx2, hkeep, hres, hcount, hpageoff, hout;
   bool timing = false;
   cudaEvent_t ev[kNumEvents] = {};
-  // batches: the next wave's pixels go up on copy_stream while the current
-  // wave computes (after its DWT, ev_dwt), into the other pixel buffer
-  // (px / px2); its DWT waits on ev_up
+  // batches: a wave's pixels go up on copy_stream (the next wave's while the
+  // current one computes), alternating between px and px2; its DWT waits
+  // on ev_up
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t ev_dwt[2] = {}, ev_up[2] = {};
+  cudaEvent_t ev_up[2] = {};
   uint8_t* wave_px = nullptr;  // the current wave's device pixels
   float stage_ms[kNumStages + 4] = {};
   uint64_t counters[8] = {};
@@ -478,7 +478,6 @@ struct Prestaged {
   size_t total;
   DevBuf* dev = nullptr;              // the wave's device pixel buffer (default: px)
   cudaEvent_t uploaded = nullptr;     // set: the pixels are already on their way (wait on it)
-  std::function<void()> after_dwt;    // called once the wave's DWT is launched
 };
 constexpr size_t kStageFailed = ~size_t(0);
 
@@ -503,7 +502,11 @@ bool needs_staging(const PageJob* j, size_t wave_host_bytes) {
   return (j->ncomp == 3 && !j->interleaved) || wave_host_bytes > kDirectCopyMax;
 }
 
-size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
+// on_staged (optional) is called, on the host thread that finished it, for
+// each page once its pixels are in `buf`, so its upload can start while the
+// other pages are still being gathered.
+size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf,
+                    const std::function<void(const PageJob*)>& on_staged = nullptr) {
   size_t total = 0, host_bytes = 0;
   std::vector<PageJob*> paged;
   for (size_t i = 0; i < n; ++i) {
@@ -511,7 +514,9 @@ size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
     PagePlan p;
     Failure f{};
     j->staged = false;
+    j->laid_out = false;
     if (!j->host_px || !build_plan(j->w, j->h, (int)j->ncomp, j->quality, j->format, &p, &f)) continue;
+    j->laid_out = true;
     j->px_off = total;
     total += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
     host_bytes += (size_t)j->w * j->h * j->ncomp;
@@ -529,14 +534,27 @@ size_t stage_pixels(jp2g_ctx* c, PageJob* const* jobs, size_t n, HostBuf& buf) {
   struct CopyTask {
     const PageJob* j;
     size_t p0, p1;  // pixel range
+    size_t page;    // index in `staged`
   };
   std::vector<CopyTask> tasks;
-  for (const PageJob* j : staged) {
+  std::unique_ptr<std::atomic<int>[]> left(new std::atomic<int>[staged.size()]);
+  for (size_t i = 0; i < staged.size(); ++i) {
+    const PageJob* j = staged[i];
     const size_t np = (size_t)j->w * j->h, step = std::max<size_t>((2u << 20) / j->ncomp, 1);
-    for (size_t p0 = 0; p0 < np; p0 += step) tasks.push_back({j, p0, std::min(np, p0 + step)});
+    int count = 0;
+    for (size_t p0 = 0; p0 < np; p0 += step, ++count) tasks.push_back({j, p0, std::min(np, p0 + step), i});
+    left[i].store(count);
   }
   parallel_for(tasks.size(), tasks.size() > 2 ? host_threads(c) : 1, [&](size_t k) {
     const CopyTask& t = tasks[k];
+    struct Done {  // the last task of a page hands it on
+      const CopyTask& t;
+      std::atomic<int>* left;
+      const std::function<void(const PageJob*)>& cb;
+      ~Done() {
+        if (cb && left[t.page].fetch_sub(1) == 1) cb(t.j);
+      }
+    } done{t, left.get(), on_staged};
     const PageJob* j = t.j;
     uint8_t* dst = staging + j->px_off;
     const size_t np = (size_t)j->w * j->h;
@@ -830,7 +848,6 @@ int run_wave(jp2g_ctx* c, PageJob* const* jobs, size_t njobs, WaveDebug* dbg,
   record(c, 1);
   // ---- colour + DWT + quantisation, one launch per level for the wave ----
   if (int rc = run_dwt_wave(c, live, dbg && dbg->raw_coefficients)) return rc;
-  if (pre && pre->after_dwt) pre->after_dwt();
   record(c, 2);
   if (dbg && dbg->stop_after_dwt) {
     if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "DWT")) return kEncodeFailed;
@@ -1182,7 +1199,6 @@ int jp2g_create(jp2g_ctx** out, int device, uint64_t hbm_budget_bytes) {
   for (auto& ev : c->ev) cudaEventCreate(&ev);
   cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
   for (int k = 0; k < 2; ++k) {
-    cudaEventCreateWithFlags(&c->ev_dwt[k], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_up[k], cudaEventDisableTiming);
   }
   *out = c;
@@ -1216,7 +1232,6 @@ void jp2g_destroy(jp2g_ctx* c) {
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   for (int k = 0; k < 2; ++k) {
-    if (c->ev_dwt[k]) cudaEventDestroy(c->ev_dwt[k]);
     if (c->ev_up[k]) cudaEventDestroy(c->ev_up[k]);
   }
   if (c->copy_stream) {
@@ -1666,14 +1681,50 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
   auto waves = form_waves(c, ptrs);
   HostBuf* bufs[2] = {&c->hpx, &c->hpx2};
   DevBuf* devs[2] = {&c->px, &c->px2};
-  // Without a budget the next wave's pixels also go up to the device while
-  // this wave computes: the helper thread stages them, waits until this
-  // wave's DWT (the last reader of the other pixel buffer two waves back) is
-  // launched, and copies them on the copy stream after it.
+  // Without a budget, each wave's pixels go to the device on a copy stream
+  // as they are gathered (page by page, while the host threads gather the
+  // rest), into one of two device pixel buffers; from the second wave on,
+  // on a helper thread while the previous wave computes. The wave's DWT
+  // waits on the copy's event.
   const bool overlap = c->budget == 0;
-  size_t staged = stage_pixels(c, waves.empty() ? nullptr : waves[0].data(),
-                               waves.empty() ? 0 : waves[0].size(), *bufs[0]);
-  bool uploaded = false;  // wave w's pixels were sent by the previous wave's helper
+  // room for wave k's pixels (an upper bound of what it stages); main thread
+  auto room_for = [&](size_t k) {
+    size_t bound = 0;
+    for (PageJob* j : waves[k])
+      if (j->host_px) bound += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
+    return bound == 0 || reserve(c, *devs[k & 1], bound);
+  };
+  // gathers wave k into bufs[k & 1] and copies it into devs[k & 1] on the
+  // copy stream; *sent tells whether every copy was issued
+  auto upload = [&](size_t k, bool* sent) {
+    HostBuf& hb = *bufs[k & 1];
+    DevBuf& dev = *devs[k & 1];
+    std::atomic<bool> ok{true};
+    const size_t total = stage_pixels(c, waves[k].data(), waves[k].size(), hb, [&](const PageJob* j) {
+      const size_t bytes = (size_t)j->w * j->h * j->ncomp;
+      if (j->px_off + bytes > dev.cap ||
+          cudaMemcpyAsync(dptr<uint8_t>(dev) + j->px_off, static_cast<const uint8_t*>(hb.p) + j->px_off, bytes,
+                          cudaMemcpyHostToDevice, c->copy_stream) != cudaSuccess)
+        ok = false;
+    });
+    if (total == kStageFailed) return total;
+    for (PageJob* j : waves[k]) {  // pages copied straight from the caller's memory
+      if (!j->laid_out || j->staged) continue;
+      const size_t bytes = (size_t)j->w * j->h * j->ncomp;
+      if (j->px_off + bytes > dev.cap ||
+          cudaMemcpyAsync(dptr<uint8_t>(dev) + j->px_off, j->host_px, bytes, cudaMemcpyHostToDevice,
+                          c->copy_stream) != cudaSuccess)
+        ok = false;
+    }
+    *sent = ok && cudaEventRecord(c->ev_up[k & 1], c->copy_stream) == cudaSuccess;
+    return total;
+  };
+  bool uploaded = false;  // wave w's pixels are on their way (ev_up)
+  size_t staged = 0;
+  if (!waves.empty()) {
+    if (overlap && room_for(0)) staged = upload(0, &uploaded);
+    else staged = stage_pixels(c, waves[0].data(), waves[0].size(), *bufs[0]);
+  }
   for (size_t w = 0; w < waves.size(); ++w) {
     auto& wave = waves[w];
     if (staged == kStageFailed) {
@@ -1682,52 +1733,19 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
     }
     size_t next_staged = 0;
     bool next_uploaded = false;
-    std::promise<bool> dwt_launched;
-    std::future<bool> dwt_future = dwt_launched.get_future();
-    bool signalled = false;
-    DevBuf* next_dev = devs[(w + 1) & 1];
-    bool next_room = false;
-    if (overlap && w + 1 < waves.size()) {
-      // room for the next wave's pixels (an upper bound of what it stages)
-      size_t bound = 0;
-      for (PageJob* j : waves[w + 1])
-        if (j->host_px) bound += ((size_t)j->w * j->h * j->ncomp + 255) & ~size_t(255);
-      next_room = bound == 0 || reserve(c, *next_dev, bound);
-    }
+    const bool next_room = overlap && w + 1 < waves.size() && room_for(w + 1);
     std::thread stager;
     if (w + 1 < waves.size()) {
-      stager = std::thread([&, w, next_dev, next_room] {
+      stager = std::thread([&, w, next_room] {
         cudaSetDevice(c->device);
-        auto& nw = waves[w + 1];
-        next_staged = stage_pixels(c, nw.data(), nw.size(), *bufs[(w + 1) & 1]);
-        const bool go = dwt_future.get();
-        if (!go || !next_room || next_staged == kStageFailed || next_staged == 0) return;
-        if (cudaStreamWaitEvent(c->copy_stream, c->ev_dwt[w & 1], 0) != cudaSuccess) return;
-        const uint8_t* pinned = static_cast<const uint8_t*>(bufs[(w + 1) & 1]->p);
-        for (PageJob* j : nw) {
-          if (!j->host_px || j->px_off + (size_t)j->w * j->h * j->ncomp > next_dev->cap) continue;
-          const uint8_t* from = j->staged ? pinned + j->px_off : j->host_px;
-          if (cudaMemcpyAsync(dptr<uint8_t>(*next_dev) + j->px_off, from, (size_t)j->w * j->h * j->ncomp,
-                              cudaMemcpyHostToDevice, c->copy_stream) != cudaSuccess)
-            return;
-        }
-        if (cudaEventRecord(c->ev_up[(w + 1) & 1], c->copy_stream) == cudaSuccess) next_uploaded = true;
+        if (next_room) next_staged = upload(w + 1, &next_uploaded);
+        else next_staged = stage_pixels(c, waves[w + 1].data(), waves[w + 1].size(), *bufs[(w + 1) & 1]);
       });
     }
     Prestaged pre{bufs[w & 1], staged};
     pre.dev = devs[w & 1];
     pre.uploaded = uploaded ? c->ev_up[w & 1] : nullptr;
-    if (overlap)
-      pre.after_dwt = [&] {
-        if (signalled) return;
-        signalled = true;
-        dwt_launched.set_value(cudaEventRecord(c->ev_dwt[w & 1], c->stream) == cudaSuccess);
-      };
     rc = run_wave_within_budget(c, wave.data(), wave.size(), &pre);
-    if (!signalled) {
-      signalled = true;
-      dwt_launched.set_value(false);  // no DWT was launched: the next wave uploads its own pixels
-    }
     if (stager.joinable()) stager.join();
     staged = next_staged;
     uploaded = next_uploaded;
@@ -1735,6 +1753,7 @@ int jp2g_encode_batch(jp2g_ctx* c, const jp2g_request* reqs, uint32_t n, uint8_t
     if (rc != JP2G_OK) break;
     add_wave_stage_times(c);
   }
+  cudaStreamSynchronize(c->copy_stream);  // an upload for a wave that did not run
   std::memcpy(c->counters, counters, sizeof counters);
   if (c->timing) {
     // batch: device stages summed over waves; host = wall time not covered

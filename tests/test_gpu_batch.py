@@ -78,15 +78,26 @@ def test_mq_blocks_per_warp_does_not_change_output(eng, bpw):
         eng.set_option(_native.OPT_MQ_BLOCKS_PER_WARP, 0)
 
 
-def test_batch_failure_is_per_page(eng):
-    pages = _mix(4, 4)
+@pytest.mark.parametrize("wave_blocks", [1, 40, 160000])
+def test_batch_failure_is_per_page(eng, wave_blocks):
+    # invalid pages hold host pixels but no place in the wave's pixel
+    # buffer: whatever wave they fall in, nothing of theirs is uploaded
+    pages = _mix(6, 4)
     bad = dict(pages[1])
     bad["ncomp"] = 2
-    bad["px"] = np.zeros(bad["w"] * bad["h"] * 2, np.uint8)
-    outs = eng.encode_batch([pages[0], bad, pages[2]])
-    assert outs[0] == _single(eng, pages[0])
-    assert isinstance(outs[1], jl.InvalidInput)
-    assert outs[2] == _single(eng, pages[2])
+    bad["px"] = np.full(bad["w"] * bad["h"] * 2, 200, np.uint8)
+    bad2 = dict(pages[3])
+    bad2["quality"] = 300
+    batch = [pages[0], bad, pages[2], bad2, pages[4], pages[5]]
+    old = eng.get_option(_native.OPT_WAVE_BLOCKS)
+    try:
+        eng.set_option(_native.OPT_WAVE_BLOCKS, wave_blocks)
+        outs = eng.encode_batch(batch)
+    finally:
+        eng.set_option(_native.OPT_WAVE_BLOCKS, old)
+    assert isinstance(outs[1], jl.InvalidInput) and isinstance(outs[3], jl.InvalidInput)
+    for k in (0, 2, 4, 5):
+        assert outs[k] == _single(eng, batch[k])
 
 
 def test_empty_batch(eng):
