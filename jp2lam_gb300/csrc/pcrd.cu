@@ -65,11 +65,19 @@ __global__ void pcrd_hull_kernel(PcrdArgs a) {
   double cw_base = o.cls == 0 ? 2.5 : (o.cls == 1 ? 1.5 : 1.0);
   double block_w = bp.is_ll ? __dmul_rn(cw_base, 1.1) : cw_base;
 
+  // The hull as a stack of points (bytes hb, distortion hd, pass count hp)
+  // with hs[k] the slope from point k-1 to point k, computed once when
+  // point k is pushed or its predecessor popped: the same operands as
+  // recomputing both slopes at every comparison, so the same bits, with
+  // about half the f64 divisions. The top point and its slope stay in
+  // registers.
   uint32_t hb[kMaxPts];
-  double hd[kMaxPts];
+  double hd[kMaxPts], hs[kMaxPts];
   uint16_t hp[kMaxPts];
-  int hn = 0;
-  hb[0] = 0; hd[0] = 0.0; hp[0] = 0; hn = 1;
+  int hn = 1;
+  hb[0] = 0; hd[0] = 0.0; hp[0] = 0; hs[0] = 0.0;
+  uint32_t tb = 0;
+  double td = 0.0, ts = 0.0;
   double cum_d = 0.0;
   for (uint32_t i = 0; i < n; ++i) {
     const PassRec r = pr[i];
@@ -88,25 +96,25 @@ __global__ void pcrd_hull_kernel(PcrdArgs a) {
     delta = __dmul_rn(delta, cp.comp_weight);
     cum_d = __dadd_rn(cum_d, delta);
     uint32_t cum = cum_len(pr, n, i, o.payload_len) + 2u;  // HEADER_OVERHEAD_BYTES
-    // push, then prune while the slope does not strictly decrease
-    hb[hn] = cum; hd[hn] = cum_d; hp[hn] = (uint16_t)(i + 1); ++hn;
-    while (hn >= 3) {
-      double sab = rd_slope(hb[hn - 3], hd[hn - 3], hb[hn - 2], hd[hn - 2]);
-      double sbc = rd_slope(hb[hn - 2], hd[hn - 2], hb[hn - 1], hd[hn - 1]);
-      if (sbc >= sab) {
-        hb[hn - 2] = hb[hn - 1]; hd[hn - 2] = hd[hn - 1]; hp[hn - 2] = hp[hn - 1];
-        --hn;
-      } else {
-        break;
-      }
+    // push, after popping the top while the slope does not strictly
+    // decrease (the slope into the new point >= the slope into the top)
+    double sn = rd_slope(tb, td, cum, cum_d);
+    while (hn >= 2 && sn >= ts) {
+      --hn;
+      tb = hb[hn - 1];
+      td = hd[hn - 1];
+      ts = hs[hn - 1];
+      sn = rd_slope(tb, td, cum, cum_d);
     }
+    hb[hn] = cum; hd[hn] = cum_d; hp[hn] = (uint16_t)(i + 1); hs[hn] = sn; ++hn;
+    tb = cum; td = cum_d; ts = sn;
   }
   // hull slopes and the component's largest finite positive slope
   double mx = 0.0;
   uint16_t* outp = a.hull_passes + d.pass_off;
   double* outs = a.hull_slope + d.pass_off;
   for (int i = 1; i < hn; ++i) {
-    double s = rd_slope(hb[i - 1], hd[i - 1], hb[i], hd[i]);
+    const double s = hs[i];
     outp[i - 1] = hp[i];
     outs[i - 1] = s;
     if (isfinite(s) && s > mx) mx = s;
@@ -225,7 +233,9 @@ __global__ void copy_bodies_kernel(const BlockDesc* blocks, const BlockKeep* kee
 void launch_pcrd(const PcrdArgs& a, cudaStream_t st) {
   if (a.nblocks == 0) return;
   cudaMemsetAsync(a.comp_max_slope, 0, sizeof(unsigned long long) * a.ncomp_keys, st);
-  const int t = 128;
+  // one warp per CTA: a page's blocks spread over all SMs, whose few f64
+  // units bound the hull's divisions
+  const int t = 32;
   const uint32_t g = (a.nblocks + t - 1) / t;
   pcrd_hull_kernel<<<g, t, 0, st>>>(a);
   pcrd_select_kernel<<<g, t, 0, st>>>(a);
