@@ -142,10 +142,12 @@ int jp2g_encode_batch(jp2g_ctx* ctx, const jp2g_request* reqs, uint32_t n, uint8
                       size_t* out_lens, int* status);
 
 /* Continuous batching. jp2g_submit validates the request (validate_image,
- * src/plan/validate.rs:4-62, before any device work) and queues it; a
- * worker thread admits queued requests into the next device wave as the
- * previous one leaves the device, up to JP2G_OPT_WAVE_BLOCKS code-blocks,
- * and a second thread completes the finished waves' tickets. The pixel
+ * src/plan/validate.rs:4-62, before any device work) and queues it. Queued
+ * requests are admitted into device waves of up to JP2G_OPT_WAVE_BLOCKS
+ * code-blocks. Without a memory budget, a stager thread admits the next wave
+ * and uploads its pixels while a worker thread runs the current one; under
+ * a budget, the worker admits each wave as the previous one leaves the
+ * device. Another thread completes the finished waves' tickets. The pixel
  * buffer must stay valid until jp2g_poll has returned the ticket's result.
  * jp2g_poll waits up to timeout_ms (< 0: no limit) and returns the
  * request's status with its codestream, or JP2G_PENDING if it is not done

@@ -101,7 +101,7 @@ struct jp2g_ctx {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   uint64_t budget = 0;
-  uint64_t allocated = 0;
+  std::atomic<uint64_t> allocated{0};  // device pool bytes (also grown by the serving stager)
   bool budget_hit = false;         // the last pool growth was refused by the budget
   uint64_t budget_wave_blocks = 0;  // most code-blocks per wave that fit the budget (0: no cap learnt)
   std::string err;  // guarded by errmu
@@ -128,16 +128,34 @@ struct jp2g_ctx {
   // uneven batches: fewer waves, fewer MQ tails); 160,000 under a budget
   int64_t opt[JP2G_NUM_OPTS] = {240000, 0, 0, 0, 0, 0, 0};
   // submit/poll: a worker thread forms waves from the queue and runs them;
-  // a finisher thread marks the finished waves' tickets done.
+  // a finisher thread marks the finished waves' tickets done. Without a
+  // memory budget a stager thread forms the waves instead: it gathers each
+  // wave's pixels into pinned memory and uploads them on its own stream
+  // while the worker runs the previous wave, through two pinned and two
+  // device pixel buffers of its own (the wave in buffer k holds it until the
+  // worker is done with it).
   std::mutex qmu;
-  std::condition_variable qcv, fcv, dcv;
+  std::condition_variable qcv, fcv, dcv, rcv;
   std::deque<std::shared_ptr<Ticket>> pending;
   std::deque<std::vector<std::shared_ptr<Ticket>>> finishing;
   std::unordered_map<uint64_t, std::shared_ptr<Ticket>> tickets;
   uint64_t next_ticket = 1;
   int inflight = 0;  // waves taken off `pending` and not yet handed to the finisher
   bool stop = false;
-  std::thread worker, finisher;
+  std::thread worker, finisher, stager;
+  struct StagedWave {
+    std::vector<std::shared_ptr<Ticket>> tickets;
+    size_t total = 0;       // stage_pixels' layout bytes
+    int buf = 0;            // serving pixel buffer pair
+    bool uploaded = false;  // the pixels are on their way (serve_ev[buf])
+  };
+  std::deque<StagedWave> staged;  // formed and gathered, not yet taken by the worker (at most one)
+  bool serve_buf_busy[2] = {false, false};
+  uint64_t serve_waves = 0;  // waves the stager has formed
+  HostBuf serve_hpx[2];
+  DevBuf serve_px[2];
+  cudaStream_t serve_stream = nullptr;
+  cudaEvent_t serve_ev[2] = {};
 };
 
 namespace {
@@ -1018,7 +1036,7 @@ void release_pools(jp2g_ctx* c) {
     b->p = nullptr;
     b->cap = 0;
   }
-  c->allocated = 0;
+  c->allocated.store(0);
 }
 
 // Admission by the device memory budget: runs a wave, and when a pool could
@@ -1198,8 +1216,10 @@ int jp2g_create(jp2g_ctx** out, int device, uint64_t hbm_budget_bytes) {
   }
   for (auto& ev : c->ev) cudaEventCreate(&ev);
   cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+  cudaStreamCreateWithFlags(&c->serve_stream, cudaStreamNonBlocking);
   for (int k = 0; k < 2; ++k) {
     cudaEventCreateWithFlags(&c->ev_up[k], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->serve_ev[k], cudaEventDisableTiming);
   }
   *out = c;
   return JP2G_OK;
@@ -1213,6 +1233,8 @@ void jp2g_destroy(jp2g_ctx* c) {
   }
   c->qcv.notify_all();
   c->fcv.notify_all();
+  c->rcv.notify_all();
+  if (c->stager.joinable()) c->stager.join();
   if (c->worker.joinable()) c->worker.join();
   if (c->finisher.joinable()) c->finisher.join();
   cudaSetDevice(c->device);
@@ -1224,19 +1246,27 @@ void jp2g_destroy(jp2g_ctx* c) {
                     &c->mqorder, &c->mqscratch, &c->recon, &c->reconblk, &c->t2pk, &c->t2bd, &c->t2pg,
                     &c->t2tmpl, &c->t2tree, &c->t2raw, &c->t2hdr, &c->t2hdrlen, &c->t2pktoff, &c->t2pagelen,
                     &c->t2pageoff, &c->t2nchunks, &c->t2chunkbase, &c->t2out};
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
+  if (c->serve_stream) {
+    cudaStreamSynchronize(c->serve_stream);
+    cudaStreamDestroy(c->serve_stream);
+  }
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
-  HostBuf* hb[] = {&c->hpx, &c->hpx2, &c->hkeep, &c->hres, &c->hcount, &c->hpageoff, &c->hout};
+  for (DevBuf& b : c->serve_px)
+    if (b.p) cudaFree(b.p);
+  HostBuf* hb[] = {&c->hpx, &c->hpx2, &c->hkeep, &c->hres, &c->hcount, &c->hpageoff, &c->hout,
+                   &c->serve_hpx[0], &c->serve_hpx[1]};
   for (HostBuf* b : hb)
     if (b->p) cudaFreeHost(b->p);
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   for (int k = 0; k < 2; ++k) {
     if (c->ev_up[k]) cudaEventDestroy(c->ev_up[k]);
-  }
-  if (c->copy_stream) {
-    cudaStreamSynchronize(c->copy_stream);
-    cudaStreamDestroy(c->copy_stream);
+    if (c->serve_ev[k]) cudaEventDestroy(c->serve_ev[k]);
   }
   cudaStreamDestroy(c->stream);
   delete c;
@@ -1788,6 +1818,52 @@ namespace {
 
 // Worker: forms a wave from the queue (FIFO, up to the wave limits), runs
 // its device phase and hands it to the finisher.
+// Takes the next wave off the queue: requests in arrival order while they
+// share a code-block size and fit the wave limits. Called with qmu held and
+// the queue not empty.
+std::vector<std::shared_ptr<Ticket>> take_wave(jp2g_ctx* c) {
+  std::vector<std::shared_ptr<Ticket>> wave;
+  uint64_t blocks = 0;
+  int cbw = 0;
+  while (!c->pending.empty() && wave.size() < kMaxWavePages) {
+    const PagePlan& p = c->pending.front()->job.plan;
+    if (!wave.empty() && (p.cbw != cbw || blocks + p.nblocks > wave_block_limit(c, p.cbw))) break;
+    cbw = p.cbw;
+    blocks += p.nblocks;
+    wave.push_back(c->pending.front());
+    c->pending.pop_front();
+  }
+  return wave;
+}
+
+// Runs one wave's pages on the device and hands the wave to the finisher.
+void run_served_wave(jp2g_ctx* c, std::vector<std::shared_ptr<Ticket>>& wave, const Prestaged* pre, int buf) {
+  std::vector<PageJob*> jobs;
+  for (auto& t : wave) jobs.push_back(&t->job);
+  int rc;
+  std::string err;
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    rc = run_wave_within_budget(c, jobs.data(), jobs.size(), pre);
+    if (rc != JP2G_OK) err = get_msg(c);
+  }
+  if (rc != JP2G_OK)
+    for (PageJob* j : jobs) {
+      j->status = rc;
+      j->err = err;
+    }
+  {
+    std::lock_guard<std::mutex> lk(c->qmu);
+    c->finishing.push_back(std::move(wave));
+    --c->inflight;
+    if (buf >= 0) c->serve_buf_busy[buf] = false;
+  }
+  c->fcv.notify_one();
+  if (buf >= 0) c->qcv.notify_all();  // the stager may use the buffer again
+}
+
+// Worker under a memory budget: forms each wave itself and runs it (its
+// pixels staged inside the wave, which may be split to fit the budget).
 void worker_loop(jp2g_ctx* c) {
   cudaSetDevice(c->device);
   for (;;) {
@@ -1796,39 +1872,101 @@ void worker_loop(jp2g_ctx* c) {
       std::unique_lock<std::mutex> lk(c->qmu);
       c->qcv.wait(lk, [&] { return c->stop || !c->pending.empty(); });
       if (c->stop && c->pending.empty()) return;
-      uint64_t blocks = 0;
-      int cbw = 0;
-      while (!c->pending.empty() && wave.size() < kMaxWavePages) {
-        const PagePlan& p = c->pending.front()->job.plan;
-        if (!wave.empty() && (p.cbw != cbw || blocks + p.nblocks > wave_block_limit(c, p.cbw)))
-          break;
-        cbw = p.cbw;
-        blocks += p.nblocks;
-        wave.push_back(c->pending.front());
-        c->pending.pop_front();
-      }
+      wave = take_wave(c);
+      ++c->inflight;
+    }
+    run_served_wave(c, wave, nullptr, -1);
+  }
+}
+
+// Stager (no budget): forms the next wave as soon as the worker has taken
+// the previous one and a pixel buffer pair is free, gathers its pixels into
+// the pair's pinned buffer and copies each page to the pair's device buffer
+// on serve_stream as soon as it is gathered.
+void stager_loop(jp2g_ctx* c) {
+  cudaSetDevice(c->device);
+  for (;;) {
+    jp2g_ctx::StagedWave sw;
+    {
+      std::unique_lock<std::mutex> lk(c->qmu);
+      c->qcv.wait(lk, [&] {
+        return (c->stop && c->pending.empty()) ||
+               (!c->pending.empty() && c->staged.empty() && !c->serve_buf_busy[c->serve_waves & 1]);
+      });
+      if (c->pending.empty()) break;  // stopping, nothing queued
+      sw.buf = (int)(c->serve_waves++ & 1);
+      c->serve_buf_busy[sw.buf] = true;
+      sw.tickets = take_wave(c);
       ++c->inflight;
     }
     std::vector<PageJob*> jobs;
-    for (auto& t : wave) jobs.push_back(&t->job);
-    int rc;
-    std::string err;
-    {
-      std::lock_guard<std::mutex> lk(c->mu);
-      rc = run_wave_within_budget(c, jobs.data(), jobs.size(), nullptr);
-      if (rc != JP2G_OK) err = get_msg(c);
+    size_t bound = 0;
+    for (auto& t : sw.tickets) {
+      jobs.push_back(&t->job);
+      if (t->job.host_px) bound += ((size_t)t->job.w * t->job.h * t->job.ncomp + 255) & ~size_t(255);
     }
-    if (rc != JP2G_OK)
-      for (PageJob* j : jobs) {
-        j->status = rc;
-        j->err = err;
+    HostBuf& hb = c->serve_hpx[sw.buf];
+    DevBuf& dev = c->serve_px[sw.buf];
+    std::atomic<bool> ok{true};
+    auto send = [&](const PageJob* j, const uint8_t* from) {
+      const size_t bytes = (size_t)j->w * j->h * j->ncomp;
+      if (j->px_off + bytes > dev.cap || cudaMemcpyAsync(dptr<uint8_t>(dev) + j->px_off, from, bytes,
+                                                         cudaMemcpyHostToDevice, c->serve_stream) != cudaSuccess)
+        ok = false;
+    };
+    if (bound > 0 && reserve(c, dev, bound)) {
+      sw.total = stage_pixels(c, jobs.data(), jobs.size(), hb, [&](const PageJob* j) {
+        send(j, static_cast<const uint8_t*>(hb.p) + j->px_off);
+      });
+      if (sw.total != kStageFailed) {
+        for (PageJob* j : jobs)  // pages copied straight from the caller's memory
+          if (j->laid_out && !j->staged) send(j, j->host_px);
+        sw.uploaded = ok && cudaEventRecord(c->serve_ev[sw.buf], c->serve_stream) == cudaSuccess;
       }
+    } else {
+      // nothing from host memory, or no room: the worker copies the pixels
+      sw.total = stage_pixels(c, jobs.data(), jobs.size(), hb);
+    }
     {
       std::lock_guard<std::mutex> lk(c->qmu);
-      c->finishing.push_back(std::move(wave));
-      --c->inflight;
+      c->staged.push_back(std::move(sw));
     }
-    c->fcv.notify_one();
+    c->rcv.notify_one();
+  }
+  c->rcv.notify_all();
+  c->fcv.notify_all();
+}
+
+// Worker with a stager: runs the staged waves in order.
+void runner_loop(jp2g_ctx* c) {
+  cudaSetDevice(c->device);
+  for (;;) {
+    jp2g_ctx::StagedWave sw;
+    {
+      std::unique_lock<std::mutex> lk(c->qmu);
+      c->rcv.wait(lk, [&] { return !c->staged.empty() || (c->stop && c->pending.empty() && c->inflight == 0); });
+      if (c->staged.empty()) return;
+      sw = std::move(c->staged.front());
+      c->staged.pop_front();
+    }
+    c->qcv.notify_all();  // the stager may form the next wave
+    if (sw.total == kStageFailed) {
+      std::lock_guard<std::mutex> lk(c->qmu);
+      for (auto& t : sw.tickets) {
+        t->job.status = kEncodeFailed;
+        t->job.err = "staging the wave's pixels failed";
+      }
+      c->finishing.push_back(std::move(sw.tickets));
+      --c->inflight;
+      c->serve_buf_busy[sw.buf] = false;
+      c->fcv.notify_one();
+      c->qcv.notify_all();
+      continue;
+    }
+    Prestaged pre{&c->serve_hpx[sw.buf], sw.total};
+    pre.dev = &c->serve_px[sw.buf];
+    pre.uploaded = sw.uploaded ? c->serve_ev[sw.buf] : nullptr;
+    run_served_wave(c, sw.tickets, &pre, sw.buf);
   }
 }
 
@@ -1877,7 +2015,12 @@ int jp2g_submit(jp2g_ctx* c, const jp2g_request* req, uint64_t* ticket) {
   {
     std::lock_guard<std::mutex> lk(c->qmu);
     if (!c->worker.joinable()) {
-      c->worker = std::thread(worker_loop, c);
+      if (c->budget == 0) {
+        c->stager = std::thread(stager_loop, c);
+        c->worker = std::thread(runner_loop, c);
+      } else {
+        c->worker = std::thread(worker_loop, c);
+      }
       c->finisher = std::thread(finisher_loop, c);
     }
     t->id = c->next_ticket++;
