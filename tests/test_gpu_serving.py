@@ -161,3 +161,57 @@ def test_destroy_with_requests_still_queued_does_not_hang():
     t0 = time.time()
     eng.close()
     assert time.time() - t0 < 60
+
+
+def test_staged_waves_alongside_direct_and_batch_calls(orc):
+    # Without a budget the stager gathers and uploads each served wave
+    # through its own pixel buffers while the worker runs the previous one;
+    # direct encodes and batches from other threads use the engine's own
+    # buffers in between. Planar RGB requests are always gathered in pinned
+    # memory, the others are copied straight from the caller's memory.
+    served = _pages(30, 7, sizes=((640, 480), (1275, 1650), (257, 129), (64, 64)))
+    for p in served[::3]:
+        if p["ncomp"] == 3:
+            p["px"] = np.ascontiguousarray(p["px"].reshape(p["h"] * p["w"], 3).T)
+            p["interleaved"] = False
+    direct = _pages(6, 8)
+    batch = _pages(8, 9, sizes=((640, 480), (300, 200)))
+    eng = jl.Engine(0)
+    results, errors = {}, []
+
+    def run(name, f):
+        try:
+            results[name] = f()
+        except Exception as e:  # reported below
+            errors.append((name, e))
+
+    def serve():
+        tickets = []
+        for p in served:
+            tickets.append(eng.submit(p))
+            time.sleep(0.003)
+        return [eng.poll(t, 120000) for t in tickets]
+
+    jobs = {
+        "served": serve,
+        "direct": lambda: [eng.encode(p["px"], p["w"], p["h"], p["ncomp"], p["quality"], p["fmt"]) for p in direct],
+        "batch": lambda: eng.encode_batch(batch),
+    }
+    try:
+        threads = [threading.Thread(target=run, args=(k, f)) for k, f in jobs.items()]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join(180)
+        assert not any(t.is_alive() for t in threads)
+        assert not errors, errors
+        for p, data in zip(served, results["served"]):
+            want = p if p.get("interleaved", True) else dict(
+                p, px=np.ascontiguousarray(p["px"].T).ravel())
+            assert data == _oracle(orc, want)
+        for p, data in zip(direct, results["direct"]):
+            assert data == _oracle(orc, p)
+        for p, data in zip(batch, results["batch"]):
+            assert data == _oracle(orc, p)
+    finally:
+        eng.close()
