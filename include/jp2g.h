@@ -161,7 +161,7 @@ int jp2g_poll(jp2g_ctx* ctx, uint64_t ticket, uint8_t** out, size_t* out_len, in
  * wave and is removed from the queue, or it had already finished and its
  * result is dropped; either way its ticket is released (the pixel buffer
  * may be reused at once; a later jp2g_poll reports an unknown ticket).
- * JP2G_PENDING: its wave is on the device or in Tier-2; the
+ * JP2G_PENDING: its wave is formed (staged, on the device or in Tier-2); the
  * result is dropped, and jp2g_poll on the ticket returns
  * JP2G_ENCODE_FAILED ("request cancelled") once the wave is done -- the
  * pixel buffer must stay valid until then. A poll already waiting on a
